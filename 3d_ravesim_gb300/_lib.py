@@ -1,0 +1,165 @@
+"""ctypes binding of librs_fresnel.so (C ABI in include/rs_fresnel.h).
+
+This is the only module that talks to the native library. There is no CPU fallback: if the
+library is missing or fails to load, every call raises RuntimeError.
+"""
+from __future__ import annotations
+
+import ctypes
+import threading
+import weakref
+from pathlib import Path
+
+import torch
+
+from . import _build
+
+RS_OK, RS_EINVAL, RS_ENOMEM, RS_ECUDA, RS_EUNSUPPORTED, RS_ETIMEOUT, RS_ECANCELLED = range(7)
+
+c_int, c_uint, c_double, c_void_p = ctypes.c_int, ctypes.c_uint, ctypes.c_double, ctypes.c_void_p
+
+
+class VoxelGeom(ctypes.Structure):
+    _fields_ = [("nz", c_int), ("ny_v", c_int), ("nx_v", c_int),
+                ("pixel_size_x", c_double), ("pixel_size_y", c_double), ("pixel_size_z", c_double),
+                ("x_pos", c_double), ("y_pos", c_double)]
+
+
+class PlasmaConsts(ctypes.Structure):
+    _fields_ = [("f1bar", c_double), ("f2eff_bar", c_double), ("zbar", c_double), ("z2bar", c_double),
+                ("energy_ev", c_double), ("planck_hc", c_double), ("r_electron_cm", c_double)]
+
+
+class DetectorGeom(ctypes.Structure):
+    _fields_ = [("dx", c_double), ("dy", c_double), ("ds_px", c_double), ("ds_py", c_double),
+                ("detector_z", c_double), ("out_x", c_int), ("out_y", c_int),
+                ("integrator", c_int), ("accumulate", c_int)]
+
+
+_P = c_void_p
+_DP = ctypes.POINTER(c_double)
+_SIGS = {
+    "rs_version": ([], ctypes.c_char_p),
+    "rs_last_error": ([], ctypes.c_char_p),
+    "rs_plan_create": ([c_int, c_int, c_uint, ctypes.POINTER(c_void_p)], c_int),
+    "rs_plan_destroy": ([_P], c_int),
+    "rs_plan_is_fast": ([_P], c_int),
+    "rs_fft2": ([_P, _P, _P, _P], c_int),
+    "rs_ifft2": ([_P, _P, _P, _P], c_int),
+    "rs_apply_cutoff": ([_P, _P, c_double, c_double, c_double, _P], c_int),
+    "rs_apply_transfer": ([_P, _P, c_double, c_double, c_double, c_double, c_double, _P], c_int),
+    "rs_propagate": ([_P, _P, _P, c_double, c_double, c_double, c_double, c_double, c_int, _P], c_int),
+    "rs_point_source": ([_P, _P, c_double, c_double, c_double, c_double, c_double, c_double, _P], c_int),
+    "rs_point_source_propagate": ([_P, _P, _P, c_double, c_double, c_double, c_double, c_double,
+                                   c_double, c_double, _P], c_int),
+    "rs_multislice_voxel": ([_P, _P, _P, _P, c_int, _P, c_int, ctypes.POINTER(VoxelGeom), c_double,
+                             c_double, c_double, c_double, _DP, _DP, c_int, c_int, _P], c_int),
+    "rs_multislice_plasma": ([_P, _P, _P, _P, _P, _P, _P, c_int, ctypes.POINTER(PlasmaConsts),
+                              ctypes.POINTER(VoxelGeom), c_double, c_double, c_double, c_double,
+                              _DP, _DP, c_int, c_int, _P], c_int),
+    "rs_detector": ([_P, _P, _P, ctypes.POINTER(DetectorGeom), _P], c_int),
+    "rs_launch_count": ([ctypes.POINTER(ctypes.c_ulonglong)], c_int),
+    "rs_plan_profile": ([_P, c_int], c_int),
+    "rs_plan_profile_read": ([_P, _DP, _DP, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
+    "rs_apply_transmission_voxel": ([_P, _P, _P, c_int, _P, c_int, ctypes.POINTER(VoxelGeom),
+                                     c_double, c_double, c_double, c_int, c_double, _P], c_int),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def library_path() -> Path:
+    return _build.LIB
+
+
+def lib() -> ctypes.CDLL:
+    """Load (building first if the sources are newer) the native library."""
+    global _lib
+    if _lib is None:
+        with _lock:
+            if _lib is None:
+                path = _build.build()
+                handle = ctypes.CDLL(str(path))
+                for name, (argtypes, restype) in _SIGS.items():
+                    fn = getattr(handle, name)
+                    fn.argtypes = argtypes
+                    fn.restype = restype
+                _lib = handle
+    return _lib
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGS)
+
+
+def check(status: int, what: str) -> None:
+    if status == RS_OK:
+        return
+    msg = lib().rs_last_error().decode(errors="replace")
+    text = f"{what}: {msg}"
+    if status == RS_EINVAL:
+        raise ValueError(text)
+    if status == RS_ECANCELLED:
+        raise InterruptedError(text)
+    if status == RS_ETIMEOUT:
+        raise TimeoutError(text)
+    if status == RS_ENOMEM:
+        raise MemoryError(text)
+    if status == RS_EUNSUPPORTED:
+        raise NotImplementedError(text)
+    raise RuntimeError(text)
+
+
+def stream_handle(device: torch.device | None = None) -> c_void_p:
+    return c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def ptr(t: torch.Tensor) -> c_void_p:
+    return c_void_p(t.data_ptr())
+
+
+class Plan:
+    """Owns one rs_plan (twiddles, transfer and geometry tables) for an (nx, ny) field."""
+
+    def __init__(self, nx: int, ny: int, device: torch.device):
+        self.nx, self.ny, self.device = int(nx), int(ny), device
+        handle = c_void_p()
+        with torch.cuda.device(device):
+            check(lib().rs_plan_create(self.nx, self.ny, 0, ctypes.byref(handle)), "rs_plan_create")
+        self.handle = handle
+        self.fast = bool(lib().rs_plan_is_fast(handle))
+        self._finalizer = weakref.finalize(self, Plan._destroy, handle, device)
+
+    @staticmethod
+    def _destroy(handle: c_void_p, device: torch.device) -> None:
+        try:
+            with torch.cuda.device(device):
+                lib().rs_plan_destroy(handle)
+        except Exception:
+            pass
+
+
+_plans: dict[tuple[int, int, int], Plan] = {}
+
+
+def plan_for(nx: int, ny: int, device: torch.device) -> Plan:
+    """Cached plan per (nx, ny, device). Plans are not shared between threads."""
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    key = (int(nx), int(ny), idx)
+    p = _plans.get(key)
+    if p is None:
+        p = Plan(nx, ny, torch.device("cuda", idx))
+        _plans[key] = p
+    return p
+
+
+def launch_count() -> int:
+    n = ctypes.c_ulonglong(0)
+    check(lib().rs_launch_count(ctypes.byref(n)), "rs_launch_count")
+    return int(n.value)
+
+
+def doubles(values) -> ctypes.Array:
+    arr = (c_double * len(values))(*[float(v) for v in values])
+    return arr

@@ -1,0 +1,732 @@
+// rs_abi.cu — plan object and the extern "C" entry points declared in include/rs_fresnel.h.
+//
+// Fast path: both axes are powers of two in [16, 16384]; a Fresnel step is one row pass and
+// one column pass (plus one row pass to return to real space at the end of a run of slices).
+// Generic path: any other size up to 6144 per axis, built from the direct-DFT and
+// elementwise kernels (still on the GPU; there is no CPU fallback).
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "rs_fresnel.h"
+#include "rs_misc.cuh"
+
+using namespace rs;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define RS_CK(call)                                                                    \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) return fail(RS_ECUDA, "%s failed: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+#define RS_TRY(expr)              \
+  do {                            \
+    int st_ = (expr);             \
+    if (st_ != RS_OK) return st_; \
+  } while (0)
+
+constexpr int kGenericMax = 6144;
+
+std::atomic<unsigned long long> g_launches{0};
+
+bool finite_pos(double v) { return std::isfinite(v) && v > 0.0; }
+
+}  // namespace
+
+namespace rs {
+void note_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+}  // namespace rs
+
+struct rs_plan {
+  int nx = 0, ny = 0, dev = 0;
+  bool fast = false;
+  void* arena = nullptr;
+  float2* tw_x = nullptr;
+  float2* tw_y = nullptr;
+  float2* ex = nullptr;
+  float2* ey = nullptr;
+  int* ylim = nullptr;
+  int* xi = nullptr;
+  float* xf = nullptr;
+  int* yi = nullptr;
+  float* yf = nullptr;
+  void* det = nullptr;
+  size_t det_cap = 0;
+  // optional per-pass event timing of the multislice loop (rs_plan_profile)
+  bool prof = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<int> ev_kind;  // 0 = row pass, 1 = column pass, per event pair
+  size_t ev_used = 0;
+};
+
+namespace {
+
+cudaStream_t as_stream(void* s) { return static_cast<cudaStream_t>(s); }
+
+int check_plan(const rs_plan* p) {
+  if (!p) return fail(RS_EINVAL, "plan is NULL");
+  int dev = -1;
+  RS_CK(cudaGetDevice(&dev));
+  if (dev != p->dev) return fail(RS_EINVAL, "plan was created on device %d but device %d is current", p->dev, dev);
+  return RS_OK;
+}
+
+int build_prop(rs_plan* p, double dx, double dy, double wl, double dz, double cutoff, bool with_h,
+               cudaStream_t s) {
+  if (!finite_pos(dx) || !finite_pos(dy)) return fail(RS_EINVAL, "dx and dy must be positive and finite (dx=%g, dy=%g)", dx, dy);
+  if (with_h && (!finite_pos(wl) || !std::isfinite(dz)))
+    return fail(RS_EINVAL, "wavelength must be positive and dz finite (wl=%g, dz=%g)", wl, dz);
+  if (std::isnan(cutoff)) return fail(RS_EINVAL, "cutoff frequency is NaN");
+  PropTabArgs a{};
+  a.nx = p->nx;
+  a.ny = p->ny;
+  a.dx = dx;
+  a.dy = dy;
+  // numpy: phase_scale = -1j*np.pi*wl*dz -> imaginary part -((pi*wl)*dz);
+  //        global_phase = exp(1j*2*np.pi/wl*dz) -> angle ((2*pi)/wl)*dz; freq_sq = 2.0*freq**2
+  a.ps = with_h ? -((M_PI * wl) * dz) : 0.0;
+  a.gphi = with_h ? ((2.0 * M_PI) / wl) * dz : 0.0;
+  a.freq_sq = 2.0 * std::pow(cutoff, 2.0);
+  a.with_h = with_h ? 1 : 0;
+  a.ex = p->ex;
+  a.ey = p->ey;
+  a.ylim = p->ylim;
+  RS_CK(launch_prop_tables(a, s));
+  return RS_OK;
+}
+
+int build_axes(rs_plan* p, const rs_voxel_geom* g, double dx, double dy, double cs, cudaStream_t s) {
+  AxisTabArgs ax{p->nx, dx, cs, g->x_pos, g->nx_v, g->pixel_size_x, p->xi, p->xf};
+  RS_CK(launch_axis_table(ax, s));
+  AxisTabArgs ay{p->ny, dy, cs, g->y_pos, g->ny_v, g->pixel_size_y, p->yi, p->yf};
+  RS_CK(launch_axis_table(ay, s));
+  return RS_OK;
+}
+
+AxisTab axis_tab(const rs_plan* p) { return AxisTab{p->xi, p->xf, p->yi, p->yf}; }
+
+// Records a start event before a pass when profiling is on; returns the pair index or -1.
+int prof_begin(rs_plan* p, int kind, cudaStream_t s) {
+  if (!p->prof) return -1;
+  if (p->ev_used + 2 > p->ev_pool.size()) {
+    for (int i = 0; i < 64; ++i) {
+      cudaEvent_t e;
+      if (cudaEventCreate(&e) != cudaSuccess) return -1;
+      p->ev_pool.push_back(e);
+    }
+  }
+  const size_t i = p->ev_used;
+  p->ev_used += 2;
+  p->ev_kind.push_back(kind);
+  cudaEventRecord(p->ev_pool[i], s);
+  return static_cast<int>(i);
+}
+
+void prof_end(rs_plan* p, int idx, cudaStream_t s) {
+  if (idx >= 0) cudaEventRecord(p->ev_pool[idx + 1], s);
+}
+
+// ---- building blocks (stream-ordered, no host sync) ----------------------------------
+int fft2_impl(rs_plan* p, const float2* in, float2* out, cudaStream_t s) {
+  if (p->fast) {
+    RowArgs r{};
+    r.in = in; r.out = out; r.ny = p->ny; r.flags = ROW_FWD; r.tw = p->tw_x;
+    RS_CK(launch_row_pass(p->nx, r, s));
+    ColArgs c{};
+    c.in = out; c.out = out; c.nx = p->nx; c.flags = COL_FWD; c.tw = p->tw_y;
+    RS_CK(launch_col_pass(p->ny, c, s));
+  } else {
+    RS_CK(launch_dft_axis(in, out, p->nx, p->ny, 0, 0, p->tw_x, 1.0f, s));
+    RS_CK(launch_dft_axis(out, out, p->nx, p->ny, 1, 0, p->tw_y, 1.0f, s));
+  }
+  return RS_OK;
+}
+
+int ifft2_impl(rs_plan* p, const float2* in, float2* out, cudaStream_t s) {
+  const float inv_n = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
+  if (p->fast) {
+    ColArgs c{};
+    c.in = in; c.out = out; c.nx = p->nx; c.flags = COL_INV | COL_SCALE; c.scale = inv_n; c.tw = p->tw_y;
+    RS_CK(launch_col_pass(p->ny, c, s));
+    RowArgs r{};
+    r.in = out; r.out = out; r.ny = p->ny; r.flags = ROW_INV; r.tw = p->tw_x;
+    RS_CK(launch_row_pass(p->nx, r, s));
+  } else {
+    RS_CK(launch_dft_axis(in, out, p->nx, p->ny, 1, 1, p->tw_y, 1.0f, s));
+    RS_CK(launch_dft_axis(out, out, p->nx, p->ny, 0, 1, p->tw_x, inv_n, s));
+  }
+  return RS_OK;
+}
+
+// Transmission of slice s (already tabulated in the plan's axis tables) and one Fresnel step
+// on the generic path: u *= T; U = FFT2(u); U *= H*mask; u = IFFT2(U).
+int generic_slice(rs_plan* p, float2* u, float2* U, const VoxelArgs* vox, const PlasmaArgs* pl,
+                  cudaStream_t s) {
+  if (vox || pl) RS_CK(launch_transmission(u, p->nx, p->ny, axis_tab(p), vox, pl, s));
+  RS_TRY(fft2_impl(p, u, U, s));
+  RS_CK(launch_transfer(U, p->nx, p->ny, p->ex, p->ey, p->ylim, 1, nullptr, s));
+  RS_TRY(ifft2_impl(p, U, u, s));
+  return RS_OK;
+}
+
+struct SliceSource {
+  // exactly one of vox / pl is used
+  bool plasma = false;
+  const char* grid = nullptr;  // voxel ids
+  int grid_signed = 0;
+  const float2* db = nullptr;
+  int n_db = 0;
+  const char* pg[4] = {nullptr, nullptr, nullptr, nullptr};  // plasma grids
+  int f64 = 1;
+  PlasmaArgs pl_base{};
+};
+
+// Shared driver of the voxel and plasma multislice entry points.
+int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const rs_voxel_geom* g,
+               double dx, double dy, double wl, double cutoff, const double* slice_dz,
+               const double* coord_scale, int s0, int s1, cudaStream_t s) {
+  if (!u || !U) return fail(RS_EINVAL, "u and U must be device pointers");
+  if (!g) return fail(RS_EINVAL, "geometry is NULL");
+  if (g->nz <= 0 || g->ny_v < 2 || g->nx_v < 2)
+    return fail(RS_EINVAL, "grid must be (nz>0, ny>=2, nx>=2), got (%d, %d, %d)", g->nz, g->ny_v, g->nx_v);
+  if (!finite_pos(g->pixel_size_x) || !finite_pos(g->pixel_size_y) || !finite_pos(g->pixel_size_z))
+    return fail(RS_EINVAL, "voxel pitches must be positive");
+  if (s0 < 0 || s1 > g->nz || s0 > s1) return fail(RS_EINVAL, "slice range [%d, %d) outside [0, %d]", s0, s1, g->nz);
+  if (!slice_dz) return fail(RS_EINVAL, "slice_dz is NULL");
+  if (!finite_pos(wl)) return fail(RS_EINVAL, "wavelength must be positive");
+  if (s0 == s1) return RS_OK;
+  const size_t plane = static_cast<size_t>(g->ny_v) * g->nx_v;
+  const float a = static_cast<float>(g->pixel_size_z / wl);
+  const float inv_n = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
+
+  double cur_dz = NAN, cur_cs = NAN;
+  for (int z = s0; z < s1; ++z) {
+    const double dz = slice_dz[z];
+    const double cs = coord_scale ? coord_scale[z] : 1.0;
+    if (!(dz == cur_dz)) {
+      RS_TRY(build_prop(p, dx, dy, wl, dz, cutoff, true, s));
+      cur_dz = dz;
+    }
+    if (!(cs == cur_cs)) {
+      if (!std::isfinite(cs)) return fail(RS_EINVAL, "coordinate scale of slice %d is not finite", z);
+      RS_TRY(build_axes(p, g, dx, dy, cs, s));
+      cur_cs = cs;
+    }
+    VoxelArgs vox{};
+    PlasmaArgs pl{};
+    if (!src.plasma) {
+      vox.slice = src.grid + plane * z * 4;
+      vox.grid_signed = src.grid_signed;
+      vox.nxv = g->nx_v;
+      vox.nyv = g->ny_v;
+      vox.db = src.db;
+      vox.n_db = src.n_db;
+      vox.a = a;
+    } else {
+      pl = src.pl_base;
+      const size_t es = src.f64 ? 8 : 4;
+      pl.ne = src.pg[0] + plane * z * es;
+      pl.ni = src.pg[1] + plane * z * es;
+      pl.te = src.pg[2] + plane * z * es;
+      pl.zs = src.pg[3] + plane * z * es;
+      pl.f64 = src.f64;
+      pl.nxv = g->nx_v;
+      pl.nyv = g->ny_v;
+      pl.a = a;
+    }
+    if (p->fast) {
+      RowArgs r{};
+      r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tw_x; r.ax = axis_tab(p);
+      r.flags = (z == s0 ? 0 : ROW_INV) | ROW_FWD | (src.plasma ? ROW_TPLASMA : ROW_TVOX);
+      r.vox = vox;
+      r.pl = pl;
+      const int er = prof_begin(p, 0, s);
+      RS_CK(launch_row_pass(p->nx, r, s));
+      prof_end(p, er, s);
+      ColArgs c{};
+      c.in = u; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_y;
+      c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
+      c.flags = COL_FWD | COL_H | COL_SCALE | COL_INV | (z == s1 - 1 ? COL_SPEC : 0);
+      const int ec = prof_begin(p, 1, s);
+      RS_CK(launch_col_pass(p->ny, c, s));
+      prof_end(p, ec, s);
+    } else {
+      RS_TRY(generic_slice(p, u, U, src.plasma ? nullptr : &vox, src.plasma ? &pl : nullptr, s));
+    }
+  }
+  if (p->fast) {
+    RowArgs r{};
+    r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tw_x; r.flags = ROW_INV;
+    RS_CK(launch_row_pass(p->nx, r, s));
+  }
+  return RS_OK;
+}
+
+// ---- detector geometry (big-wave/propagation.py:766-815, 818-833, 949-992) -------------
+struct DetTables {
+  std::vector<double> xdet, ydet, yw;
+  std::vector<float> xw;
+  std::vector<int> xptr, xcell, yptr, ycell;
+};
+
+void area_axis(int out_n, double ds, int grid_n, double sp, std::vector<double>& det,
+               std::vector<double>& lo, std::vector<double>& hi, std::vector<long>& ilo,
+               std::vector<double>& flo, std::vector<long>& ihi, std::vector<double>& fhi) {
+  det.resize(out_n); lo.resize(out_n); hi.resize(out_n);
+  ilo.resize(out_n); flo.resize(out_n); ihi.resize(out_n); fhi.resize(out_n);
+  const double gl = (static_cast<double>(-(grid_n / 2)) - 0.5) * sp;
+  const double gr = gl + static_cast<double>(grid_n) * sp;
+  for (int i = 0; i < out_n; ++i) {
+    det[i] = (static_cast<double>(i) - static_cast<double>(out_n / 2)) * ds;
+    lo[i] = det[i] - ds * 0.5;
+    hi[i] = det[i] + ds * 0.5;
+    const double clo = std::min(std::max(lo[i], gl), gr);
+    double chi = std::min(std::max(hi[i], gl), gr);
+    chi = std::max(chi, clo);
+    const double slo = (clo - gl) / sp, shi = (chi - gl) / sp;
+    ilo[i] = static_cast<long>(std::floor(slo));
+    ihi[i] = static_cast<long>(std::floor(shi));
+    flo[i] = slo - static_cast<double>(ilo[i]);
+    fhi[i] = shi - static_cast<double>(ihi[i]);
+    if (ilo[i] >= grid_n) { ilo[i] = grid_n; flo[i] = 0.0; }
+    if (ihi[i] >= grid_n) { ihi[i] = grid_n; fhi[i] = 0.0; }
+  }
+}
+
+void build_area_v1(int nx, int ny, const rs_detector_geom& g, DetTables& t) {
+  std::vector<double> xlo, xhi, ylo, yhi, fx0, fx1, fy0, fy1;
+  std::vector<long> ix0, ix1, iy0, iy1;
+  area_axis(g.out_x, g.ds_px, nx, g.dx, t.xdet, xlo, xhi, ix0, fx0, ix1, fx1);
+  area_axis(g.out_y, g.ds_py, ny, g.dy, t.ydet, ylo, yhi, iy0, fy0, iy1, fy1);
+  // x: integral = dx*(sum_{i0<=k<i1} I_k - f0*I_i0 + f1*I_i1), terms at index nx dropped
+  t.xptr.assign(1, 0);
+  for (int o = 0; o < g.out_x; ++o) {
+    const long i0 = ix0[o], i1 = ix1[o];
+    for (long k = i0; k <= i1 && k < nx; ++k) {
+      double w = (k < i1) ? 1.0 : 0.0;
+      if (k == i0) w -= fx0[o];
+      if (k == i1) w += fx1[o];
+      if (w != 0.0) {
+        t.xcell.push_back(static_cast<int>(k));
+        t.xw.push_back(static_cast<float>(w * g.dx));
+      }
+    }
+    t.xptr.push_back(static_cast<int>(t.xcell.size()));
+  }
+  // y: per grid row, detector rows with positive overlap (searchsorted right/left as in 1035-1036)
+  std::vector<std::vector<std::pair<int, double>>> per(g.out_y);
+  const double gyl = (static_cast<double>(-(ny / 2)) - 0.5) * g.dy;
+  for (int gy = 0; gy < ny; ++gy) {
+    const double cl = gyl + static_cast<double>(gy) * g.dy;
+    const double ch = cl + g.dy;
+    const int first = static_cast<int>(std::upper_bound(yhi.begin(), yhi.end(), cl) - yhi.begin());
+    const int end = static_cast<int>(std::lower_bound(ylo.begin(), ylo.end(), ch) - ylo.begin());
+    for (int oy = first; oy < end; ++oy) {
+      const double ov = std::min(ch, yhi[oy]) - std::max(cl, ylo[oy]);
+      if (ov > 0) per[oy].push_back({gy, ov});
+    }
+  }
+  t.yptr.assign(1, 0);
+  for (int oy = 0; oy < g.out_y; ++oy) {
+    for (auto& e : per[oy]) { t.ycell.push_back(e.first); t.yw.push_back(e.second); }
+    t.yptr.push_back(static_cast<int>(t.ycell.size()));
+  }
+}
+
+void build_legacy(int nx, int ny, const rs_detector_geom& g, DetTables& t) {
+  auto ranges = [](int out_n, int grid_n, double ds, double sp, std::vector<double>& det,
+                   std::vector<long>& lo, std::vector<long>& hi) {
+    det.resize(out_n); lo.resize(out_n); hi.resize(out_n);
+    for (int i = 0; i < out_n; ++i) {
+      det[i] = (static_cast<double>(i) - static_cast<double>(out_n / 2)) * ds;
+      long l = static_cast<long>(std::trunc((det[i] - ds * 0.5) / sp)) + grid_n / 2;
+      long h = static_cast<long>(std::trunc((det[i] + ds * 0.5) / sp)) + grid_n / 2;
+      lo[i] = std::min<long>(std::max<long>(l, 0), grid_n);
+      hi[i] = std::min<long>(std::max<long>(h, 0), grid_n);
+    }
+  };
+  std::vector<long> lx, hx, ly, hy;
+  ranges(g.out_x, nx, g.ds_px, g.dx, t.xdet, lx, hx);
+  ranges(g.out_y, ny, g.ds_py, g.dy, t.ydet, ly, hy);
+  t.xptr.assign(1, 0);
+  for (int o = 0; o < g.out_x; ++o) {
+    for (long k = lx[o]; k < hx[o]; ++k) { t.xcell.push_back(static_cast<int>(k)); t.xw.push_back(1.0f); }
+    t.xptr.push_back(static_cast<int>(t.xcell.size()));
+  }
+  // rows gy with lo_y[oy] <= gy < hi_y[oy] (searchsorted right on both, 884-885)
+  const double w = g.dx * g.dy;
+  t.yptr.assign(1, 0);
+  for (int oy = 0; oy < g.out_y; ++oy) {
+    for (long gy = ly[oy]; gy < hy[oy]; ++gy) { t.ycell.push_back(static_cast<int>(gy)); t.yw.push_back(w); }
+    t.yptr.push_back(static_cast<int>(t.ycell.size()));
+  }
+}
+
+size_t align8(size_t v) { return (v + 7) & ~static_cast<size_t>(7); }
+
+}  // namespace
+
+// ======================================================================== extern "C"
+extern "C" {
+
+const char* rs_version(void) { return "rs_fresnel 0.1 sm_103a"; }
+
+const char* rs_last_error(void) { return g_err.c_str(); }
+
+int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
+  (void)flags;
+  if (!out) return fail(RS_EINVAL, "out is NULL");
+  *out = nullptr;
+  if (nx <= 0 || ny <= 0) return fail(RS_EINVAL, "nx and ny must be positive, got nx=%d, ny=%d", nx, ny);
+  const bool fast = fast_size(nx) && fast_size(ny);
+  if (!fast && (nx > kGenericMax || ny > kGenericMax))
+    return fail(RS_EUNSUPPORTED, "size %dx%d: axes must be powers of two in [16, 16384] or at most %d",
+                nx, ny, kGenericMax);
+  rs_plan* p = new rs_plan();
+  p->nx = nx;
+  p->ny = ny;
+  p->fast = fast;
+  cudaError_t e = cudaGetDevice(&p->dev);
+  if (e != cudaSuccess) { delete p; return fail(RS_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e)); }
+  // arena: tw_x, ex (nx float2) | tw_y, ey (ny float2) | ylim, xi (nx int) | xf (nx) | yi (ny) | yf (ny)
+  const size_t bytes = align8(sizeof(float2) * 2 * nx) + align8(sizeof(float2) * 2 * ny) +
+                       align8(sizeof(int) * 2 * nx) + align8(sizeof(float) * nx) +
+                       align8(sizeof(int) * ny) + align8(sizeof(float) * ny);
+  e = cudaMalloc(&p->arena, bytes);
+  if (e != cudaSuccess) { delete p; return fail(RS_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
+  char* c = static_cast<char*>(p->arena);
+  p->tw_x = reinterpret_cast<float2*>(c); c += align8(sizeof(float2) * nx);
+  p->ex = reinterpret_cast<float2*>(c); c += align8(sizeof(float2) * nx);
+  p->tw_y = reinterpret_cast<float2*>(c); c += align8(sizeof(float2) * ny);
+  p->ey = reinterpret_cast<float2*>(c); c += align8(sizeof(float2) * ny);
+  p->ylim = reinterpret_cast<int*>(c); c += align8(sizeof(int) * nx);
+  p->xi = reinterpret_cast<int*>(c); c += align8(sizeof(int) * nx);
+  p->xf = reinterpret_cast<float*>(c); c += align8(sizeof(float) * nx);
+  p->yi = reinterpret_cast<int*>(c); c += align8(sizeof(int) * ny);
+  p->yf = reinterpret_cast<float*>(c);
+  e = launch_twiddles(p->tw_x, nx, 0);
+  if (e == cudaSuccess) e = launch_twiddles(p->tw_y, ny, 0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+  if (e != cudaSuccess) {
+    cudaFree(p->arena);
+    delete p;
+    return fail(RS_ECUDA, "twiddle setup: %s", cudaGetErrorString(e));
+  }
+  *out = p;
+  return RS_OK;
+}
+
+int rs_plan_destroy(rs_plan* p) {
+  if (!p) return RS_OK;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev != p->dev) cudaSetDevice(p->dev);
+  for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
+  cudaError_t e1 = cudaFree(p->arena);
+  cudaError_t e2 = p->det ? cudaFree(p->det) : cudaSuccess;
+  if (dev != p->dev) cudaSetDevice(dev);
+  delete p;
+  if (e1 != cudaSuccess || e2 != cudaSuccess) return fail(RS_ECUDA, "cudaFree failed during plan destroy");
+  return RS_OK;
+}
+
+int rs_plan_is_fast(const rs_plan* p) { return p && p->fast ? 1 : 0; }
+
+int rs_launch_count(unsigned long long* out) {
+  if (!out) return fail(RS_EINVAL, "out is NULL");
+  *out = g_launches.load(std::memory_order_relaxed);
+  return RS_OK;
+}
+
+int rs_plan_profile(rs_plan* p, int enable) {
+  RS_TRY(check_plan(p));
+  p->prof = enable != 0;
+  p->ev_used = 0;
+  p->ev_kind.clear();
+  return RS_OK;
+}
+
+int rs_plan_profile_read(rs_plan* p, double* row_ms, double* col_ms, int* n_row, int* n_col) {
+  RS_TRY(check_plan(p));
+  if (!row_ms || !col_ms || !n_row || !n_col) return fail(RS_EINVAL, "NULL output pointer");
+  *row_ms = *col_ms = 0.0;
+  *n_row = *n_col = 0;
+  for (size_t k = 0; k < p->ev_kind.size(); ++k) {
+    RS_CK(cudaEventSynchronize(p->ev_pool[2 * k + 1]));
+    float ms = 0.f;
+    RS_CK(cudaEventElapsedTime(&ms, p->ev_pool[2 * k], p->ev_pool[2 * k + 1]));
+    if (p->ev_kind[k] == 0) { *row_ms += ms; ++*n_row; } else { *col_ms += ms; ++*n_col; }
+  }
+  p->ev_used = 0;
+  p->ev_kind.clear();
+  return RS_OK;
+}
+
+int rs_fft2(rs_plan* p, const void* in, void* out, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!in || !out) return fail(RS_EINVAL, "NULL field pointer");
+  return fft2_impl(p, static_cast<const float2*>(in), static_cast<float2*>(out), as_stream(stream));
+}
+
+int rs_ifft2(rs_plan* p, const void* in, void* out, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!in || !out) return fail(RS_EINVAL, "NULL field pointer");
+  return ifft2_impl(p, static_cast<const float2*>(in), static_cast<float2*>(out), as_stream(stream));
+}
+
+int rs_apply_cutoff(rs_plan* p, void* U, double freq, double dx, double dy, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!U) return fail(RS_EINVAL, "NULL field pointer");
+  cudaStream_t s = as_stream(stream);
+  RS_TRY(build_prop(p, dx, dy, 1.0, 0.0, freq, false, s));
+  RS_CK(launch_transfer(static_cast<float2*>(U), p->nx, p->ny, p->ex, p->ey, p->ylim, 0, nullptr, s));
+  return RS_OK;
+}
+
+int rs_apply_transfer(rs_plan* p, void* U, double dx, double dy, double wl, double dz, double cutoff,
+                      void* stream) {
+  RS_TRY(check_plan(p));
+  if (!U) return fail(RS_EINVAL, "NULL field pointer");
+  cudaStream_t s = as_stream(stream);
+  RS_TRY(build_prop(p, dx, dy, wl, dz, cutoff, true, s));
+  RS_CK(launch_transfer(static_cast<float2*>(U), p->nx, p->ny, p->ex, p->ey, p->ylim, 1, nullptr, s));
+  return RS_OK;
+}
+
+int rs_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double wl, double dz,
+                 double cutoff, int skip_fft, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
+  float2* u = static_cast<float2*>(u_);
+  float2* U = static_cast<float2*>(U_);
+  cudaStream_t s = as_stream(stream);
+  RS_TRY(build_prop(p, dx, dy, wl, dz, cutoff, true, s));
+  if (p->fast) {
+    const float inv_n = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
+    if (!skip_fft) {
+      RowArgs r{};
+      r.in = u; r.out = U; r.ny = p->ny; r.flags = ROW_FWD; r.tw = p->tw_x;
+      RS_CK(launch_row_pass(p->nx, r, s));
+    }
+    ColArgs c{};
+    c.in = U; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_y;
+    c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
+    c.flags = (skip_fft ? 0 : COL_FWD) | COL_H | COL_SPEC | COL_SCALE | COL_INV;
+    RS_CK(launch_col_pass(p->ny, c, s));
+    RowArgs r{};
+    r.in = u; r.out = u; r.ny = p->ny; r.flags = ROW_INV; r.tw = p->tw_x;
+    RS_CK(launch_row_pass(p->nx, r, s));
+  } else {
+    if (!skip_fft) RS_TRY(fft2_impl(p, u, U, s));
+    RS_CK(launch_transfer(U, p->nx, p->ny, p->ex, p->ey, p->ylim, 1, nullptr, s));
+    RS_TRY(ifft2_impl(p, U, u, s));
+  }
+  return RS_OK;
+}
+
+static int point_args(rs_plan* p, double dx, double dy, double xs, double ys, double z, double wl,
+                      PointSrcArgs& a) {
+  if (!finite_pos(dx) || !finite_pos(dy) || !finite_pos(wl))
+    return fail(RS_EINVAL, "dx, dy and wavelength must be positive");
+  if (!std::isfinite(z) || !std::isfinite(xs) || !std::isfinite(ys)) return fail(RS_EINVAL, "non-finite source geometry");
+  a.dx = dx; a.dy = dy; a.xs = xs; a.ys = ys;
+  a.z2 = z * z;
+  a.k = (2.0 * M_PI) / wl;  // imaginary part of numpy's 2j*np.pi/wl
+  a.half_nx = static_cast<double>(p->nx) / 2.0;
+  a.half_ny = static_cast<double>(p->ny) / 2.0;
+  return RS_OK;
+}
+
+int rs_point_source(rs_plan* p, void* u, double dx, double dy, double xs, double ys, double z,
+                    double wl, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!u) return fail(RS_EINVAL, "NULL field pointer");
+  PointSrcArgs a{};
+  RS_TRY(point_args(p, dx, dy, xs, ys, z, wl, a));
+  RS_CK(launch_point_source(static_cast<float2*>(u), p->nx, p->ny, a, as_stream(stream)));
+  return RS_OK;
+}
+
+int rs_point_source_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double xs,
+                              double ys, double z, double wl, double cutoff, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
+  float2* u = static_cast<float2*>(u_);
+  float2* U = static_cast<float2*>(U_);
+  cudaStream_t s = as_stream(stream);
+  PointSrcArgs a{};
+  RS_TRY(point_args(p, dx, dy, xs, ys, z, wl, a));
+  RS_TRY(build_prop(p, dx, dy, wl, 0.0, cutoff, false, s));
+  if (p->fast) {
+    RowArgs r{};
+    r.out = U; r.ny = p->ny; r.flags = ROW_SRC | ROW_FWD; r.tw = p->tw_x; r.ps = a;
+    RS_CK(launch_row_pass(p->nx, r, s));
+    ColArgs c{};
+    c.in = U; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_y; c.ylim = p->ylim;
+    c.scale = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
+    c.flags = COL_FWD | COL_MASK | COL_SPEC | COL_SCALE | COL_INV;
+    RS_CK(launch_col_pass(p->ny, c, s));
+    RowArgs r2{};
+    r2.in = u; r2.out = u; r2.ny = p->ny; r2.flags = ROW_INV; r2.tw = p->tw_x;
+    RS_CK(launch_row_pass(p->nx, r2, s));
+  } else {
+    RS_CK(launch_point_source(u, p->nx, p->ny, a, s));
+    RS_TRY(fft2_impl(p, u, U, s));
+    RS_CK(launch_transfer(U, p->nx, p->ny, p->ex, p->ey, p->ylim, 0, nullptr, s));
+    RS_TRY(ifft2_impl(p, U, u, s));
+  }
+  return RS_OK;
+}
+
+int rs_multislice_voxel(rs_plan* p, void* u, void* U, const void* grid, int grid_signed, const float* db,
+                        int n_db, const rs_voxel_geom* geom, double dx, double dy, double wl,
+                        double cutoff, const double* slice_dz, const double* coord_scale,
+                        int slice_begin, int slice_end, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!grid || !db) return fail(RS_EINVAL, "grid and db must be device pointers");
+  if (n_db < 1) return fail(RS_EINVAL, "n_db must be >= 1");
+  SliceSource src;
+  src.grid = static_cast<const char*>(grid);
+  src.grid_signed = grid_signed;
+  src.db = reinterpret_cast<const float2*>(db);
+  src.n_db = n_db;
+  return multislice(p, static_cast<float2*>(u), static_cast<float2*>(U), src, geom, dx, dy, wl, cutoff,
+                    slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
+}
+
+int rs_multislice_plasma(rs_plan* p, void* u, void* U, const void* ne, const void* ni, const void* te,
+                         const void* zstar, int grid_f64, const rs_plasma_consts* pc,
+                         const rs_voxel_geom* geom, double dx, double dy, double wl, double cutoff,
+                         const double* slice_dz, const double* coord_scale, int slice_begin,
+                         int slice_end, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!ne || !ni || !te || !zstar) return fail(RS_EINVAL, "plasma grids must be device pointers");
+  if (!pc || !finite_pos(pc->energy_ev)) return fail(RS_EINVAL, "energy must be positive");
+  SliceSource src;
+  src.plasma = true;
+  src.pg[0] = static_cast<const char*>(ne);
+  src.pg[1] = static_cast<const char*>(ni);
+  src.pg[2] = static_cast<const char*>(te);
+  src.pg[3] = static_cast<const char*>(zstar);
+  src.f64 = grid_f64 ? 1 : 0;
+  // big-wave/plasma.py:407-433 with densities pre-scaled by 1e-20 inside the kernel
+  const double lamb_cm = 1.0e-8 * pc->planck_hc / pc->energy_ev;
+  const double pref = pc->r_electron_cm * lamb_cm * lamb_cm / (2.0 * M_PI);
+  const double nu = pc->energy_ev / 4.135667e-15;
+  PlasmaArgs& b = src.pl_base;
+  b.pref = pref;
+  b.f1bar = pc->f1bar;
+  b.f2eff = pc->f2eff_bar;
+  b.zbar_pos = pc->zbar > 0.0 ? 1.0 : 0.0;
+  b.inv_zbar = pc->zbar > 0.0 ? 1.0 / pc->zbar : 0.0;
+  b.z2bar_pos = pc->z2bar > 0.0 ? 1.0 : 0.0;
+  b.cff = 3.7e8 * pc->z2bar / (std::sqrt(11604.5) * nu * nu * nu) * lamb_cm / (4.0 * M_PI) * 1e40;
+  return multislice(p, static_cast<float2*>(u), static_cast<float2*>(U), src, geom, dx, dy, wl, cutoff,
+                    slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
+}
+
+int rs_apply_transmission_voxel(rs_plan* p, void* u, const void* grid, int grid_signed, const float* db,
+                                int n_db, const rs_voxel_geom* g, double dx, double dy, double wl,
+                                int slice, double coord_scale, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!u || !grid || !db || !g) return fail(RS_EINVAL, "NULL pointer argument");
+  if (slice < 0 || slice >= g->nz) return fail(RS_EINVAL, "slice %d outside [0, %d)", slice, g->nz);
+  if (g->ny_v < 2 || g->nx_v < 2 || n_db < 1) return fail(RS_EINVAL, "bad grid shape or table");
+  if (!finite_pos(wl)) return fail(RS_EINVAL, "wavelength must be positive");
+  cudaStream_t s = as_stream(stream);
+  RS_TRY(build_axes(p, g, dx, dy, coord_scale, s));
+  VoxelArgs vox{};
+  vox.slice = static_cast<const char*>(grid) + static_cast<size_t>(g->ny_v) * g->nx_v * slice * 4;
+  vox.grid_signed = grid_signed;
+  vox.nxv = g->nx_v;
+  vox.nyv = g->ny_v;
+  vox.db = reinterpret_cast<const float2*>(db);
+  vox.n_db = n_db;
+  vox.a = static_cast<float>(g->pixel_size_z / wl);
+  RS_CK(launch_transmission(static_cast<float2*>(u), p->nx, p->ny, axis_tab(p), &vox, nullptr, s));
+  return RS_OK;
+}
+
+int rs_detector(rs_plan* p, const void* u, double* out, const rs_detector_geom* g, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!u || !out || !g) return fail(RS_EINVAL, "NULL pointer argument");
+  if (g->out_x <= 0 || g->out_y <= 0) return fail(RS_EINVAL, "detector output must be non-empty");
+  if (!finite_pos(g->dx) || !finite_pos(g->dy) || !finite_pos(g->ds_px) || !finite_pos(g->ds_py))
+    return fail(RS_EINVAL, "detector and grid spacings must be positive");
+  if (!std::isfinite(g->detector_z) || g->detector_z == 0.0) return fail(RS_EINVAL, "detector z must be finite and non-zero");
+  DetTables t;
+  if (g->integrator == 0) build_area_v1(p->nx, p->ny, *g, t);
+  else if (g->integrator == 1) build_legacy(p->nx, p->ny, *g, t);
+  else return fail(RS_EINVAL, "unknown integrator %d", g->integrator);
+  const size_t o_xdet = 0;
+  const size_t o_ydet = o_xdet + align8(t.xdet.size() * 8);
+  const size_t o_yw = o_ydet + align8(t.ydet.size() * 8);
+  const size_t o_xw = o_yw + align8(t.yw.size() * 8);
+  const size_t o_xptr = o_xw + align8(t.xw.size() * 4);
+  const size_t o_xcell = o_xptr + align8(t.xptr.size() * 4);
+  const size_t o_yptr = o_xcell + align8(t.xcell.size() * 4);
+  const size_t o_ycell = o_yptr + align8(t.yptr.size() * 4);
+  const size_t total = o_ycell + align8(t.ycell.size() * 4) + 8;
+  std::vector<char> host(total, 0);
+  auto put = [&](size_t off, const void* src, size_t n) { if (n) std::memcpy(host.data() + off, src, n); };
+  put(o_xdet, t.xdet.data(), t.xdet.size() * 8);
+  put(o_ydet, t.ydet.data(), t.ydet.size() * 8);
+  put(o_yw, t.yw.data(), t.yw.size() * 8);
+  put(o_xw, t.xw.data(), t.xw.size() * 4);
+  put(o_xptr, t.xptr.data(), t.xptr.size() * 4);
+  put(o_xcell, t.xcell.data(), t.xcell.size() * 4);
+  put(o_yptr, t.yptr.data(), t.yptr.size() * 4);
+  put(o_ycell, t.ycell.data(), t.ycell.size() * 4);
+  cudaStream_t s = as_stream(stream);
+  if (total > p->det_cap) {
+    if (p->det) RS_CK(cudaFree(p->det));  // cudaFree waits for work still using the old buffer
+    p->det = nullptr;
+    p->det_cap = 0;
+    cudaError_t e = cudaMalloc(&p->det, total);
+    if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc(%zu) for detector tables: %s", total, cudaGetErrorString(e));
+    p->det_cap = total;
+  }
+  char* d = static_cast<char*>(p->det);
+  RS_CK(cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, s));
+  DetArgs a{};
+  a.u = static_cast<const float2*>(u);
+  a.out = out;
+  a.nx = p->nx;
+  a.out_x = g->out_x;
+  a.out_y = g->out_y;
+  a.xdet = reinterpret_cast<const double*>(d + o_xdet);
+  a.ydet = reinterpret_cast<const double*>(d + o_ydet);
+  a.yw = reinterpret_cast<const double*>(d + o_yw);
+  a.xw = reinterpret_cast<const float*>(d + o_xw);
+  a.xptr = reinterpret_cast<const int*>(d + o_xptr);
+  a.xcell = reinterpret_cast<const int*>(d + o_xcell);
+  a.yptr = reinterpret_cast<const int*>(d + o_yptr);
+  a.ycell = reinterpret_cast<const int*>(d + o_ycell);
+  a.z = g->detector_z;
+  a.accumulate = g->accumulate;
+  // Pageable host->device copies are staged before cudaMemcpyAsync returns, so `host` may be
+  // released now; the kernel is ordered after the copy on the same stream.
+  RS_CK(launch_detector(a, s));
+  return RS_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,136 @@
+// rs_common.cuh — complex64 helpers and in-register radix-2/4/8/16 DFT butterflies.
+//
+// Sign convention: forward transforms use exp(-2*pi*i*j*k/N) (scipy.fft.fft2, as called
+// by big-wave/vector.py:341-343); inverse ones use exp(+2*pi*i*j*k/N) and are
+// unnormalised here (the 1/N of scipy.fft.ifft2 is applied by the callers).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace rs {
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+// a * conj(b)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
+}
+// multiply by -i (forward) or +i (inverse)
+template <bool INV>
+__device__ __forceinline__ float2 mul_mi(float2 a) {
+  return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// cos(pi/8), sin(pi/8), sqrt(2)/2 (mathematical constants, correctly rounded to float).
+constexpr float kC8 = 0.92387953251128675613f;
+constexpr float kS8 = 0.38268343236508977173f;
+constexpr float kR2 = 0.70710678118654752440f;
+
+// Multiply by W16^m = exp(-+2*pi*i*m/16) for the m used inside the 4x4 radix-16 butterfly.
+template <int M, bool INV>
+__device__ __forceinline__ float2 tw16(float2 a) {
+  if constexpr (M == 0) {
+    return a;
+  } else if constexpr (M == 4) {
+    return mul_mi<INV>(a);
+  } else if constexpr (M == 2) {
+    // fwd: c(1 - i); inv: c(1 + i)
+    return INV ? make_float2(kR2 * (a.x - a.y), kR2 * (a.x + a.y))
+               : make_float2(kR2 * (a.x + a.y), kR2 * (a.y - a.x));
+  } else if constexpr (M == 6) {
+    // fwd: c(-1 - i); inv: c(-1 + i)
+    return INV ? make_float2(-kR2 * (a.x + a.y), kR2 * (a.x - a.y))
+               : make_float2(kR2 * (a.y - a.x), -kR2 * (a.x + a.y));
+  } else {
+    // generic: M in {1, 3, 9}
+    constexpr float wr = (M == 1) ? kC8 : (M == 3) ? kS8 : -kC8;
+    constexpr float wi0 = (M == 1) ? -kS8 : (M == 3) ? -kC8 : kS8;  // forward imaginary part
+    constexpr float wi = INV ? -wi0 : wi0;
+    return cmul(a, make_float2(wr, wi));
+  }
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft2(float2& a0, float2& a1) {
+  const float2 t = a0;
+  a0 = cadd(t, a1);
+  a1 = csub(t, a1);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2& a0, float2& a1, float2& a2, float2& a3) {
+  const float2 t0 = cadd(a0, a2), t1 = csub(a0, a2);
+  const float2 t2 = cadd(a1, a3), t3 = mul_mi<INV>(csub(a1, a3));
+  a0 = cadd(t0, t2);
+  a2 = csub(t0, t2);
+  a1 = cadd(t1, t3);
+  a3 = csub(t1, t3);
+}
+
+// Natural-order in, natural-order out.
+template <bool INV>
+__device__ __forceinline__ void dft8(float2 (&a)[8]) {
+  dft4<INV>(a[0], a[2], a[4], a[6]);  // E0..E3
+  dft4<INV>(a[1], a[3], a[5], a[7]);  // O0..O3
+  a[3] = tw16<2, INV>(a[3]);          // W8^1 = W16^2
+  a[5] = tw16<4, INV>(a[5]);          // W8^2 = W16^4
+  a[7] = tw16<6, INV>(a[7]);          // W8^3 = W16^6
+  float2 y[8];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    y[k] = cadd(a[2 * k], a[2 * k + 1]);
+    y[k + 4] = csub(a[2 * k], a[2 * k + 1]);
+  }
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = y[k];
+}
+
+// 16-point DFT as 4x4: column DFT4s, inner twiddles W16^(r2*k1), row DFT4s, transpose.
+template <bool INV>
+__device__ __forceinline__ void dft16(float2 (&a)[16]) {
+#pragma unroll
+  for (int r2 = 0; r2 < 4; ++r2) dft4<INV>(a[r2], a[4 + r2], a[8 + r2], a[12 + r2]);
+  a[5] = tw16<1, INV>(a[5]);
+  a[9] = tw16<2, INV>(a[9]);
+  a[13] = tw16<3, INV>(a[13]);
+  a[6] = tw16<2, INV>(a[6]);
+  a[10] = tw16<4, INV>(a[10]);
+  a[14] = tw16<6, INV>(a[14]);
+  a[7] = tw16<3, INV>(a[7]);
+  a[11] = tw16<6, INV>(a[11]);
+  a[15] = tw16<9, INV>(a[15]);
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) dft4<INV>(a[4 * k1], a[4 * k1 + 1], a[4 * k1 + 2], a[4 * k1 + 3]);
+  float2 y[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) y[k1 + 4 * k2] = a[4 * k1 + k2];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) a[k] = y[k];
+}
+
+// Radix-R DFT on the R registers v[OFF .. OFF+R-1] of a 16-register array.
+template <int R, bool INV, int OFF>
+__device__ __forceinline__ void dft_slice(float2 (&v)[16]) {
+  if constexpr (R == 16) {
+    dft16<INV>(v);
+  } else if constexpr (R == 8) {
+    float2 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = v[OFF + i];
+    dft8<INV>(a);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[OFF + i] = a[i];
+  } else if constexpr (R == 4) {
+    dft4<INV>(v[OFF], v[OFF + 1], v[OFF + 2], v[OFF + 3]);
+  } else if constexpr (R == 2) {
+    dft2<INV>(v[OFF], v[OFF + 1]);
+  }
+}
+
+}  // namespace rs

@@ -1,0 +1,57 @@
+// rs_misc.cuh — table builders, generic-size DFT, elementwise and detector kernels.
+#pragma once
+#include "rs_kernels.cuh"
+
+namespace rs {
+
+// Transfer-function tables for one (dx, dy, wl, dz, cutoff) (big-wave/propagation.py:427-441).
+struct PropTabArgs {
+  int nx, ny;
+  double dx, dy;
+  double ps;       // -(pi*wl)*dz  (imaginary part of numpy's phase_scale)
+  double gphi;     // ((2*pi)/wl)*dz (global phase)
+  double freq_sq;  // 2.0*freq**2
+  int with_h;      // 0: only the cutoff limits are built
+  float2* ex;
+  float2* ey;
+  int* ylim;
+};
+
+// Sample coordinate table for one axis (big-wave/optical_element.py:538-546, 555-563).
+struct AxisTabArgs {
+  int n;            // sim points on this axis
+  double spacing;   // sim spacing
+  double cs;        // coordinate scale
+  double pos;       // x_pos / y_pos
+  int len;          // voxel count on this axis
+  double pitch;     // voxel pitch
+  int* idx;
+  float* frac;
+};
+
+struct DetArgs {
+  const float2* u;
+  double* out;
+  int nx, out_x, out_y;
+  const int* xptr; const int* xcell; const float* xw;
+  const int* yptr; const int* ycell; const double* yw;
+  const double* xdet; const double* ydet;
+  double z;
+  int accumulate;
+};
+
+cudaError_t launch_twiddles(float2* tw, int n, cudaStream_t s);
+cudaError_t launch_prop_tables(const PropTabArgs& a, cudaStream_t s);
+cudaError_t launch_axis_table(const AxisTabArgs& a, cudaStream_t s);
+// Direct O(n^2) DFT along rows (axis 0) or columns (axis 1); inv uses exp(+...). scale multiplies the output.
+cudaError_t launch_dft_axis(const float2* in, float2* out, int nx, int ny, int axis, int inv,
+                            const float2* tw, float scale, cudaStream_t s);
+cudaError_t launch_transfer(float2* U, int nx, int ny, const float2* ex, const float2* ey,
+                            const int* ylim, int with_h, float2* spec_copy, cudaStream_t s);
+cudaError_t launch_scale(float2* u, size_t n, float scale, cudaStream_t s);
+cudaError_t launch_point_source(float2* u, int nx, int ny, const PointSrcArgs& p, cudaStream_t s);
+cudaError_t launch_transmission(float2* u, int nx, int ny, const AxisTab& ax, const VoxelArgs* vox,
+                                const PlasmaArgs* pl, cudaStream_t s);
+cudaError_t launch_detector(const DetArgs& a, cudaStream_t s);
+
+}  // namespace rs

@@ -1,0 +1,28 @@
+"""GPU drop-in for big-wave's PointSource in 2D (big-wave/source.py:44-113)."""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+from .propagation import SimParams, grid_density_check_2d, point_source_propagate_2d
+
+
+@dataclass
+class PointSource:
+    """Point source at (x, y, z); propagate_to initialises exp(2 pi i r/wl)/r at z_out, applies
+    the circular frequency cutoff, and leaves U holding the cut-off spectrum."""
+
+    x: float
+    z: float
+    y: float = 0.0
+
+    def propagate_to(self, z_out: float, sim_params: SimParams, cutoff_freq: float, u, U, history) -> None:
+        dz = z_out - self.z
+        if not sim_params.is_2d:
+            raise NotImplementedError("the GB300 PointSource implements the 2D path (ny > 1)")
+        if sim_params.use_fresnel_scaling:
+            raise NotImplementedError("Fresnel-scaled plane initialisation is not part of this build")
+        if history is not None:
+            raise NotImplementedError("analytic source history is not part of this build")
+        grid_density_check_2d(dz, self.x, sim_params.nx, sim_params.dx, self.y, sim_params.ny,
+                              sim_params.get_dy(), sim_params.wl)
+        point_source_propagate_2d(u, U, dz, self.x, self.y, sim_params, cutoff_freq)

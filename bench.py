@@ -1,0 +1,442 @@
+"""Benchmark: fused multislice slice-steps/s at 4096^2 complex64 on GB300.
+
+Workload (one "step"): the Talbot-Lau single-source configuration at 4096 x 4096 complex64 —
+point source 0.5 m upstream (exp(2 pi i r/wl)/r, FP64 phase), pi-shift Si phase grating,
+512 x 1 um Gaussian-blob voxel sample, absorption grating at the first fractional Talbot
+distance, free space to the detector, area_v1 detector — run through the package's public API
+(Sample.apply / propagate_2d / square_and_downsample_2d) on inputs already resident in HBM.
+value = transmission slices per second (514 per step: 1 + 512 + 1); the source, free-space legs
+and detector are inside the timed region but not counted.
+
+Also reported: the same workload end to end with host inputs (e2e), the unfused "plain" form on
+the same GPU (our own FFT passes as separate kernels, and a cuFFT-based variant via torch.fft),
+the dominant kernels' achieved HBM bandwidth vs the measured peak, the CPU oracle on the host
+cores, and the FP64 relative L2 error of a truncated run.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "fused slice-steps/s at 4096^2 c64 (Talbot-Lau, 512-slice blob sample)"
+UNIT = "slice-steps/s"
+# fast-wave (CUDA + cuFFT) published 43.25 ms per layer at 4096^2 c64 (RTX 5070 Ti Laptop)
+PUBLISHED_MS_PER_LAYER = 43.25
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=4096, help="field size (default 4096)")
+    ap.add_argument("--slices", type=int, default=512)
+    ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/cpu/accuracy legs")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------------------- helpers
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[3:7]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        return float(json.loads(path.read_text())["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------------------ our arm
+class Pipeline:
+    """The Talbot-Lau run through the public API on one device."""
+
+    def __init__(self, rs, wl, device):
+        import torch
+        self.rs, self.w, self.dev = rs, wl, device
+        self.p = wl.params
+        n = self.p.nx
+        self.u = rs.GpuVector.zeros(n * n, device)
+        self.U = rs.GpuVector.zeros(n * n, device)
+        self.det = None
+        for el in wl.elements:  # upload grids once: inputs resident in HBM
+            el.grid = torch.from_numpy(np.ascontiguousarray(el.grid).view(np.int32)).to(device)
+            el.grid_is_signed = False
+
+    def run(self, det_out=None):
+        rs, p, w = self.rs, self.p, self.w
+        u, U = self.u, self.U
+        z = w.z_first
+        rs.propagation.point_source_propagate_2d(u, U, z - w.source_xyz[2], w.source_xyz[0], w.source_xyz[1], p,
+                                                 w.cutoff)
+        valid = False
+        for el in w.elements:
+            if z < el.z_start:
+                rs.propagate_2d(u, U, p.dx, p.get_dy(), p.wl, el.z_start - z, p.chunk_size, w.cutoff, p.nx, p.ny,
+                                skip_fft=valid)
+            el.apply(u, U, p, w.cutoff, 0, None)
+            valid = True
+            z = el.z_start + el.get_thickness()
+        rs.propagate_2d(u, U, p.dx, p.get_dy(), p.wl, p.z_detector - z, p.chunk_size, w.cutoff, p.nx, p.ny,
+                        skip_fft=True)
+        return rs.propagation.square_and_downsample_2d_device(u, p, p.z_detector, out=det_out)
+
+
+def l2_flush_buffer(torch, device):
+    return torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
+
+
+def time_steps(torch, fn, steps, flush, stream):
+    """Sum of per-step CUDA-event times; the L2 flush between steps is outside the events."""
+    total = 0.0
+    for _ in range(steps):
+        flush.fill_(1.0)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        b.synchronize()
+        total += a.elapsed_time(b)
+    return total
+
+
+def plain_slice_rate(rs, torch, wl, device, slices: int, use_cufft: bool) -> float:
+    """Unfused form on the same GPU: per slice T multiply, FFT2, H*mask, IFFT2 as separate
+    launches (fast-wave's per-slice sequence, fast-wave/src/simulation.cpp:597-733)."""
+    lib = rs._lib
+    p = wl.params
+    n = p.nx
+    sample = wl.elements[1]
+    plan = lib.plan_for(n, n, device)
+    u = torch.ones(n * n, dtype=torch.complex64, device=device)
+    U = torch.empty_like(u)
+    geom = lib.VoxelGeom(int(sample.grid.shape[0]), int(sample.grid.shape[1]), int(sample.grid.shape[2]),
+                         sample.pixel_size_x, sample.pixel_size_y or sample.pixel_size_x, sample.pixel_size_z, 0.0, 0.0)
+    _, db = sample._device_inputs(device)
+    st = lib.stream_handle()
+    L = lib.lib()
+
+    def one(k):
+        lib.check(L.rs_apply_transmission_voxel(plan.handle, lib.ptr(u), lib.ptr(sample.grid), 0, lib.ptr(db),
+                                                len(sample.db_list), geom, p.dx, p.dx, p.wl, k, 1.0, st), "T")
+        if use_cufft:
+            Uv = torch.fft.fft2(u.view(n, n))
+            lib.check(L.rs_apply_transfer(plan.handle, lib.ptr(Uv), p.dx, p.dx, p.wl, sample.pixel_size_z,
+                                          wl.cutoff, st), "H")
+            u.copy_(torch.fft.ifft2(Uv).view(-1))
+        else:
+            lib.check(L.rs_fft2(plan.handle, lib.ptr(u), lib.ptr(U), st), "fft2")
+            lib.check(L.rs_apply_transfer(plan.handle, lib.ptr(U), p.dx, p.dx, p.wl, sample.pixel_size_z,
+                                          wl.cutoff, st), "H")
+            lib.check(L.rs_ifft2(plan.handle, lib.ptr(U), lib.ptr(u), st), "ifft2")
+
+    for k in range(3):
+        one(k)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for k in range(slices):
+        one(k % int(sample.grid.shape[0]))
+    b.record()
+    b.synchronize()
+    return slices / (a.elapsed_time(b) / 1e3)
+
+
+def cpu_baseline(n: int, samples: int = 2) -> dict:
+    """The oracle's complex64 slice-step (big-wave's NumpyVector path restated) on the host, at the
+    benchmark's field size, scipy.fft with its default single worker as big-wave calls it."""
+    from oracle import bigwave_oracle as orc
+    rs_wl = importlib.import_module("3d_ravesim_gb300.workloads")
+    w = rs_wl.talbot_lau(n=n, slices=8, blobs=20)
+    s = w.elements[1]
+    p = w.params
+    grid = np.asarray(s.grid)
+    u = np.ones((n, n), np.complex64)
+    t0 = time.perf_counter()
+    for k in range(samples):
+        t = orc.sample_transmission(grid[k], s.db_list, n, n, p.dx, p.dx, s.pixel_size_x, s.pixel_size_y,
+                                    s.pixel_size_z, p.wl)
+        u = (u * t).astype(np.complex64)
+        u, _ = orc.propagate_2d(u, p.dx, p.dx, p.wl, s.pixel_size_z, w.cutoff)
+    dt = time.perf_counter() - t0
+    return {"value": samples / dt, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"{samples} Sample slice-steps at {n}^2 complex64 (oracle restatement of big-wave's "
+                      f"NumpyVector path, scipy.fft default 1 worker), {dt:.1f} s"}
+
+
+def accuracy_check(rs, torch, device, n: int, slices: int = 4) -> dict:
+    """Relative L2 of field and detector intensity vs the FP64 oracle on the benchmark geometry
+    truncated to `slices` sample slices (the full 512-slice FP64 run takes hours on the CPU)."""
+    from scipy import fft as spfft
+
+    from oracle import bigwave_oracle as orc
+    wlmod = importlib.import_module("3d_ravesim_gb300.workloads")
+    w = wlmod.talbot_lau(n=n, slices=slices)
+    pipe = Pipeline(rs, w, device)
+    det = pipe.run()
+    torch.cuda.synchronize()
+    gpu_u = pipe.u.to_numpy().reshape(n, n)
+    gpu_det = det.cpu().numpy()
+    p = w.params
+    with spfft.set_workers(os.cpu_count() or 1):
+        z = w.z_first
+        u, U = orc.point_source_2d(n, n, p.dx, p.dx, z, 0.0, 0.0, p.wl, w.cutoff)
+        valid = False
+        for el in w.elements:
+            if z < el.z_start:
+                u, U = orc.propagate_2d(u, p.dx, p.dx, p.wl, el.z_start - z, w.cutoff, U=U if valid else None,
+                                        skip_fft=valid)
+            grid = np.asarray(el.grid.cpu().numpy() if hasattr(el.grid, "cpu") else el.grid).view(np.uint32)
+            u, U = orc.sample_apply_2d(u, grid, el.db_list, p.dx, p.dx, p.wl, w.cutoff, el.pixel_size_x,
+                                       el.pixel_size_y or el.pixel_size_x, el.pixel_size_z)
+            valid = True
+            z = el.z_start + el.get_thickness()
+        u, U = orc.propagate_2d(u, p.dx, p.dx, p.wl, p.z_detector - z, w.cutoff, U=U, skip_fft=True)
+    ref_det = orc.detector_area_v1(u, p.dx, p.dx, p.detector_pixel_size_x, p.detector_pixel_size_y,
+                                   gpu_det.shape[1], gpu_det.shape[0], p.z_detector)
+    return {"case": f"Talbot-Lau {n}^2 truncated to {slices} sample slices vs FP64 oracle",
+            "field_rel_l2": orc.relative_l2(gpu_u, u),
+            "intensity_rel_l2": orc.relative_l2(np.abs(gpu_u) ** 2, np.abs(u) ** 2),
+            "detector_rel_l2": orc.relative_l2(gpu_det, ref_det)}
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    rs = importlib.import_module("3d_ravesim_gb300")
+    rs.build()
+    wlmod = importlib.import_module("3d_ravesim_gb300.workloads")
+    w = wlmod.talbot_lau(n=args.n, slices=args.slices)
+    pipe = Pipeline(rs, w, device)
+    stream = torch.cuda.current_stream(device)
+    flush = l2_flush_buffer(torch, device)
+    det = torch.zeros((int(w.params.get_detector_size_y() // w.params.detector_pixel_size_y),
+                       int(w.params.get_detector_size_x() // w.params.detector_pixel_size_x)),
+                      dtype=torch.float64, device=device)
+    for _ in range(args.warmup):
+        pipe.run(det)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    launches0 = rs._lib.launch_count()
+    barrier()
+    with ClockSampler(local) as clocks:
+        total_ms = time_steps(torch, lambda: pipe.run(det), args.steps, flush, stream)
+    barrier()
+    launches = rs._lib.launch_count() - launches0
+    t = torch.tensor([total_ms], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    slices_per_step = w.slice_count
+    value = world * slices_per_step * args.steps / (total_ms / 1e3)
+
+    # dominant kernels: per-pass CUDA-event timing of one run (same stream)
+    plan = rs._lib.plan_for(w.params.nx, w.params.ny, device)
+    L = rs._lib.lib()
+    rs._lib.check(L.rs_plan_profile(plan.handle, 1), "profile")
+    flush.fill_(1.0)
+    pipe.run(det)
+    import ctypes
+    row_ms, col_ms = ctypes.c_double(), ctypes.c_double()
+    nr, nc = ctypes.c_int(), ctypes.c_int()
+    rs._lib.check(L.rs_plan_profile_read(plan.handle, ctypes.byref(row_ms), ctypes.byref(col_ms), ctypes.byref(nr),
+                                         ctypes.byref(nc)), "profile_read")
+    rs._lib.check(L.rs_plan_profile(plan.handle, 0), "profile")
+    n = w.params.nx
+    field_bytes = 8 * n * n
+    peak, peak_kind = measured_peak_hbm()
+    row_avg = row_ms.value / max(nr.value, 1)
+    col_avg = col_ms.value / max(nc.value, 1)
+    # algorithmic bytes per launch: read + write of the field (16 B/pixel); the row pass also reads
+    # the voxel slice it gathers (4 B per voxel of the (y_len, x_len) plane)
+    vox = w.info["voxel_grid"]
+    row_bytes = 2 * field_bytes + 4 * vox[1] * vox[2]
+    col_bytes = 2 * field_bytes
+    row_gbs = row_bytes / (row_avg * 1e-3) / 1e9
+    col_gbs = col_bytes / (col_avg * 1e-3) / 1e9
+    dom = "col_pass" if col_ms.value >= row_ms.value else "row_pass"
+    achieved = col_gbs if dom == "col_pass" else row_gbs
+    roofline = {"bound": "hbm", "kernel": f"{dom} (fused {'column FFT*H*IFFT' if dom == 'col_pass' else 'row IFFT*T*FFT'})",
+                "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "peak_kind": peak_kind, "traffic": None,
+                "row_pass": {"avg_us": round(row_avg * 1e3, 2), "GB_s": round(row_gbs, 1), "launches": nr.value,
+                             "algorithmic_bytes": row_bytes},
+                "col_pass": {"avg_us": round(col_avg * 1e3, 2), "GB_s": round(col_gbs, 1), "launches": nc.value,
+                             "algorithmic_bytes": col_bytes},
+                "slice_step_frac": round((2 * field_bytes * 2) / ((row_avg + col_avg) * 1e-3) / 1e9 / peak, 4)}
+
+    line = {"metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": round(value / (1e3 / PUBLISHED_MS_PER_LAYER), 2),
+            "dtype": "c64 (fp32 complex)", "data": "synthetic (seeded Talbot-Lau: point source, gratings, "
+            "200-blob voxel sample)",
+            "config": {"workload": f"talbot_lau_{n}x{n}_c64", "nx": n, "ny": n, "slices_per_step": slices_per_step,
+                       "sample_slices": args.slices, "voxel_grid": vox, "energy_ev": w.info["energy_ev"],
+                       "l2": "256 MiB buffer written between timed steps (flush outside the events)",
+                       "parallelism": f"replicas x{world} (one field per GPU)"},
+            "roofline": roofline, "gpu_launches": launches, "clocks": clocks.summary()}
+
+    if rank == 0 and not args.no_extras:
+        # e2e: host (pinned) voxel grids copied in and the detector image copied out every step
+        host_grids = [torch.from_numpy(np.ascontiguousarray(el.grid.cpu().numpy())).pin_memory() for el in w.elements]
+        host_det = torch.empty(det.shape, dtype=torch.float64).pin_memory()
+        h2d = sum(g.numel() * 4 for g in host_grids)
+        d2h = host_det.numel() * 8
+
+        def e2e_step():
+            for el, hg in zip(w.elements, host_grids):
+                el.grid.copy_(hg, non_blocking=True)
+            pipe.run(det)
+            host_det.copy_(det, non_blocking=True)
+        e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms = time_steps(torch, e2e_step, args.steps, flush, stream)
+        line["e2e"] = {"value": round(slices_per_step * args.steps / (e2e_ms / 1e3), 2), "unit": UNIT,
+                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                       "path": "Sample.apply/propagate_2d/square_and_downsample_2d (C ABI) with pinned host grids"}
+        # plain (unfused) comparators on the same GPU
+        plain = plain_slice_rate(rs, torch, w, device, 64, use_cufft=False)
+        cufft = plain_slice_rate(rs, torch, w, device, 64, use_cufft=True)
+        fused_rate = slices_per_step / (row_ms.value + col_ms.value) * 1e3 if (nr.value and nc.value) else None
+        line["plain"] = {"own_fft_unfused": round(plain, 1), "cufft_unfused": round(cufft, 1),
+                         "fused_sample_slices": round(fused_rate, 1) if fused_rate else None, "unit": UNIT,
+                         "note": "unfused = T kernel, FFT2, H*mask, IFFT2 as separate launches per slice"}
+        line["cpu_baseline"] = cpu_baseline(n)
+        line["accuracy"] = accuracy_check(rs, torch, device, min(n, 4096))
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+# ----------------------------------------------------------------------- reference arm
+def run_reference(args):
+    """The reference's CPU algorithm (the oracle restatement of big-wave's NumpyVector path) on the
+    host cores, scipy.fft with all host threads; one step = one Sample slice-step at 4096^2 c64."""
+    rank = int(os.environ.get("RANK", 0))
+    if rank != 0:
+        return
+    from scipy import fft as spfft
+
+    from oracle import bigwave_oracle as orc
+    wlmod = importlib.import_module("3d_ravesim_gb300.workloads")
+    n = args.n
+    w = wlmod.talbot_lau(n=n, slices=8, blobs=20)
+    s = w.elements[1]
+    p = w.params
+    grid = np.asarray(s.grid)
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    u = np.ones((n, n), np.complex64)
+
+    def step(k):
+        nonlocal u
+        t = orc.sample_transmission(grid[k % grid.shape[0]], s.db_list, n, n, p.dx, p.dx, s.pixel_size_x,
+                                    s.pixel_size_y, s.pixel_size_z, p.wl)
+        u = (u * t).astype(np.complex64)
+        u, _ = orc.propagate_2d(u, p.dx, p.dx, p.wl, s.pixel_size_z, w.cutoff)
+
+    with spfft.set_workers(cores):
+        for k in range(args.warmup):
+            step(k)
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            step(k)
+        dt = time.perf_counter() - t0
+    value = args.steps / dt
+    line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+            "data": "synthetic", "config": {"workload": f"talbot_lau_{n}x{n}_c64", "step": "one Sample slice-step"},
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} Sample slice-steps at {n}^2 c64, scipy.fft workers={cores}"},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

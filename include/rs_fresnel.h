@@ -1,0 +1,179 @@
+/*
+ * rs_fresnel.h — C ABI of the GB300 (sm_103a) multislice Fresnel propagation library.
+ *
+ * This is the drop-in boundary for big-wave's 2D hot path (RAVE-SIM). Every entry
+ * point below replaces one function of big-wave's Python API; the citation after
+ * each declaration names the reference function (file:line, paths relative to the
+ * RAVE-SIM repository root) whose semantics it reproduces.
+ *
+ * Conventions
+ *  - Fields are complex64 (interleaved float re, im), row-major (ny rows of nx
+ *    columns), exactly the memory order of big-wave's NumpyVector
+ *    (big-wave/vector.py:319-347: vec.reshape(ny, nx)). All field, grid and
+ *    output pointers are DEVICE pointers owned by the caller.
+ *  - Scalars (dx, dy, wl, dz, cutoff, ...) are in metres / 1 per metre, FP64, with
+ *    the same meaning as the reference arguments.
+ *  - Every call is stream-ordered on `stream` (a cudaStream_t passed as void*;
+ *    NULL = legacy default stream) and never synchronises the device.
+ *  - Every call returns an rs_status; on failure rs_last_error() returns a
+ *    thread-local message. Nothing calls exit() (contrast fast-wave's
+ *    fwcuda/types.hpp:226-238).
+ *  - A plan owns its twiddle/transfer/geometry tables (allocated once in
+ *    rs_plan_create). A plan must not be used concurrently from two streams.
+ */
+#ifndef RS_FRESNEL_H
+#define RS_FRESNEL_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rs_status {
+  RS_OK = 0,
+  RS_EINVAL = 1,      /* bad argument / shape (Python maps to ValueError)        */
+  RS_ENOMEM = 2,      /* device allocation failed                                  */
+  RS_ECUDA = 3,       /* a CUDA runtime call failed                                */
+  RS_EUNSUPPORTED = 4,/* size/dtype outside what this build implements             */
+  RS_ETIMEOUT = 5,    /* a bounded device wait gave up                             */
+  RS_ECANCELLED = 6   /* host cancel flag observed between slices                  */
+} rs_status;
+
+typedef struct rs_plan rs_plan;
+
+/* Library version string, e.g. "rs_fresnel 0.1 sm_103a". */
+const char* rs_version(void);
+
+/* Thread-local message describing the last failed call on this host thread. */
+const char* rs_last_error(void);
+
+/* Create a plan for fields of nx columns by ny rows on the current CUDA device.
+ * Replaces the per-call setup of big-wave/propagation.py:396-442 (fftfreq tables,
+ * chunk validation) and fast-wave's FFT<S> plan (fast-wave/src/fft.cpp:6-28).
+ * flags: reserved, pass 0. */
+int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out);
+int rs_plan_destroy(rs_plan* plan);
+/* 1 when both axes use the fused Stockham kernels, 0 when the generic DFT path is used. */
+int rs_plan_is_fast(const rs_plan* plan);
+
+/* Unnormalised forward 2D DFT, out may equal in.
+ * Replaces NumpyVector.fft2 = scipy.fft.fft2 (big-wave/vector.py:341-343). */
+int rs_fft2(rs_plan* plan, const void* in, void* out, void* stream);
+
+/* Inverse 2D DFT with 1/(nx*ny) normalisation, out may equal in.
+ * Replaces NumpyVector.ifft2 = scipy.fft.ifft2 (big-wave/vector.py:345-347). */
+int rs_ifft2(rs_plan* plan, const void* in, void* out, void* stream);
+
+/* Zero spectrum bins with kx^2+ky^2 > 2*freq^2 (kx = fftfreq(nx)/dx, FP64 test).
+ * Replaces apply_frequency_cutoff_2d (big-wave/propagation.py:298-326). */
+int rs_apply_cutoff(rs_plan* plan, void* U, double freq, double dx, double dy,
+                    void* stream);
+
+/* One Fresnel step: u <- IFFT2[mask * exp(2 pi i dz/wl) * exp(-i pi wl dz (kx^2+ky^2)) * FFT2[u]];
+ * afterwards U holds the spectrum of the new u. skip_fft != 0 means U already holds
+ * FFT2(u) and the forward transform is skipped.
+ * Replaces propagate_2d (big-wave/propagation.py:396-442). */
+int rs_propagate(rs_plan* plan, void* u, void* U, double dx, double dy, double wl,
+                 double dz, double cutoff, int skip_fft, void* stream);
+
+/* Spherical wave u = exp(2 pi i r/wl)/r from a point source at (xs, ys) a distance z
+ * upstream; x = (ix - nx/2)*dx - xs. The phase is reduced in FP64 (carrier split).
+ * Replaces propagate_analytically_2d (big-wave/propagation.py:458-484). */
+int rs_point_source(rs_plan* plan, void* u, double dx, double dy, double xs,
+                    double ys, double z, double wl, void* stream);
+
+/* PointSource.propagate_to in 2D without Fresnel scaling: analytic init, FFT2, circular
+ * cutoff, IFFT2; U is left holding the cut-off spectrum.
+ * Replaces big-wave/source.py:97-107 (after grid_density_check_2d, done by the caller). */
+int rs_point_source_propagate(rs_plan* plan, void* u, void* U, double dx, double dy,
+                              double xs, double ys, double z, double wl, double cutoff,
+                              void* stream);
+
+/* Geometry of a voxel Sample (big-wave/optical_element.py:383-412, 502-546). */
+typedef struct rs_voxel_geom {
+  int nz, ny_v, nx_v;        /* grid shape (z, y, x)                                   */
+  double pixel_size_x;       /* voxel pitch x [m]                                       */
+  double pixel_size_y;       /* voxel pitch y [m] (already resolved: 0 -> pixel_size_x) */
+  double pixel_size_z;       /* slice thickness [m] (material_factor thickness)        */
+  double x_pos, y_pos;       /* phase-stepping offsets for this iteration [m]          */
+} rs_voxel_geom;
+
+/* Fused multislice through a voxel Sample, slices [slice_begin, slice_end):
+ * per slice u *= material_factor(bilinear(db[grid[z]]), pixel_size_z, wl), then one
+ * Fresnel step of slice_dz[s] with circular cutoff. grid is uint32/int32 material ids
+ * (device), db is (n_db) x (delta, beta) float32 pairs (device, index 0 = vacuum).
+ * slice_dz (host, nz entries) are the effective step lengths; coord_scale (host, nz
+ * entries, or NULL for all 1.0) are the transverse coordinate scales of each slice.
+ * u_spectral != 0 is not supported (u is spatial on entry). Afterwards u is spatial and
+ * U holds FFT2(u).
+ * Replaces Sample._apply_2d (big-wave/optical_element.py:502-596) together with
+ * material_factor (39-42) and the propagate_2d call per slice (585-592). */
+int rs_multislice_voxel(rs_plan* plan, void* u, void* U, const void* grid, int grid_signed,
+                        const float* db, int n_db, const rs_voxel_geom* geom,
+                        double dx, double dy, double wl, double cutoff,
+                        const double* slice_dz, const double* coord_scale,
+                        int slice_begin, int slice_end, void* stream);
+
+/* Plasma model scalars per energy (big-wave/plasma_sample.py:68-83, plasma.py:241-266).
+ * planck_hc [eV*Angstrom] and r_electron_cm [cm] are the CODATA values the caller's
+ * nist_lookup uses (nist_lookup/nist_lookup/physical_constants.py: PLANCK_HC, R_ELECTRON_CM). */
+typedef struct rs_plasma_consts {
+  double f1bar, f2eff_bar, zbar, z2bar;
+  double energy_ev;
+  double planck_hc, r_electron_cm;
+} rs_plasma_consts;
+
+/* Fused multislice through a PlasmaSample: per voxel corner, delta/beta come from
+ * (n_e, n_i, T_e, Z*) grids (float64 or float32, device; grid_f64 selects) by the
+ * free-electron + bound-electron + Kramers model, then bilinear interpolation, zero
+ * outside the grid, material_factor, Fresnel step.
+ * Replaces PlasmaSample._apply_2d (big-wave/plasma_sample.py:126-233) and
+ * plasma_delta_beta_grid_multi (big-wave/plasma.py:380-434). */
+int rs_multislice_plasma(rs_plan* plan, void* u, void* U, const void* ne, const void* ni,
+                         const void* te, const void* zstar, int grid_f64,
+                         const rs_plasma_consts* pc, const rs_voxel_geom* geom,
+                         double dx, double dy, double wl, double cutoff,
+                         const double* slice_dz, const double* coord_scale,
+                         int slice_begin, int slice_end, void* stream);
+
+/* Detector geometry (big-wave/propagation.py:766-815 _detector_geometry). */
+typedef struct rs_detector_geom {
+  double dx, dy;             /* grid spacings [m]                                      */
+  double ds_px, ds_py;       /* effective detector pixel sizes [m]                     */
+  double detector_z;         /* effective distance for the obliquity cosine [m]        */
+  int out_x, out_y;          /* detector shape (columns, rows)                          */
+  int integrator;            /* 0 = area_v1, 1 = legacy_fastwave                        */
+  int accumulate;            /* 1: out += image (incoherent sum), 0: out = image        */
+} rs_detector_geom;
+
+/* |u|^2 integrated over detector pixels times the obliquity cosine; out is float64
+ * (out_y x out_x, device). area_v1 = separable exact overlap areas; legacy_fastwave =
+ * truncated index ranges. Replaces square_and_downsample_2d
+ * (big-wave/propagation.py:1113-1130) -> _area_v1_stream (995-1110) and
+ * _legacy_fastwave_stream (836-946). */
+int rs_detector(rs_plan* plan, const void* u, double* out, const rs_detector_geom* g,
+                void* stream);
+
+/* Tracing (counterpart of fast-wave's CudaTimerSection, fast-wave/src/simulation.cpp:14-33):
+ * total number of kernels this library has launched in the process ... */
+int rs_launch_count(unsigned long long* out);
+/* ... and optional CUDA-event timing of every row / column pass of the multislice loops.
+ * rs_plan_profile(plan, 1) starts recording (clearing earlier records); rs_plan_profile_read
+ * waits for the recorded passes and returns their summed milliseconds and counts, then clears. */
+int rs_plan_profile(rs_plan* plan, int enable);
+int rs_plan_profile_read(rs_plan* plan, double* row_ms, double* col_ms, int* n_row, int* n_col);
+
+/* Plain (unfused) forms used as the in-repo comparator: T multiply, H multiply. */
+int rs_apply_transmission_voxel(rs_plan* plan, void* u, const void* grid, int grid_signed,
+                                const float* db, int n_db, const rs_voxel_geom* geom,
+                                double dx, double dy, double wl, int slice, double coord_scale,
+                                void* stream);
+int rs_apply_transfer(rs_plan* plan, void* U, double dx, double dy, double wl, double dz,
+                      double cutoff, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RS_FRESNEL_H */
