@@ -16,9 +16,11 @@ PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 CSRC = PKG / "csrc"
 INCLUDE = ROOT / "include"
-BUILD = PKG / "_build"
+# RS_BUILD_DIR / RS_NVCC_EXTRA select another output directory and extra nvcc flags (e.g. a
+# -DRS_PACKED_F32X2=0 variant built side by side for comparison).
+BUILD = Path(os.environ.get("RS_BUILD_DIR", PKG / "_build"))
 LIB = BUILD / "librs_fresnel.so"
-SOURCES = ["rs_rows.cu", "rs_cols.cu", "rs_misc.cu", "rs_abi.cu"]
+SOURCES = ["rs_pass_pow2.cu", "rs_pass_pow3.cu", "rs_dispatch.cu", "rs_misc.cu", "rs_abi.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 
@@ -34,11 +36,15 @@ def common_flags() -> list[str]:
         "-std=c++17", "-O3", ARCH, "-lineinfo",
         "-Xcompiler", "-fPIC,-ffp-contract=off",
         f"-I{INCLUDE}", f"-I{CSRC}",
+        *os.environ.get("RS_NVCC_EXTRA", "").split(),
     ]
 
 
 def _stale() -> bool:
     if not LIB.exists():
+        return True
+    flags_file = BUILD / "flags.txt"
+    if not flags_file.exists() or flags_file.read_text() != " ".join(common_flags()):
         return True
     t = LIB.stat().st_mtime
     deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
@@ -74,6 +80,7 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}{r.stderr}")
     os.replace(tmp, LIB)
+    (BUILD / "flags.txt").write_text(" ".join(common_flags()))
     return LIB
 
 

@@ -407,24 +407,29 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   p->fast = fast;
   cudaError_t e = cudaGetDevice(&p->dev);
   if (e != cudaSuccess) { delete p; return fail(RS_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e)); }
-  // arena: tw_x, ex (nx float2) | tw_y, ey (ny float2) | ylim, xi (nx int) | xf (nx) | yi (ny) | yf (ny)
-  const size_t bytes = align8(sizeof(float2) * 2 * nx) + align8(sizeof(float2) * 2 * ny) +
+  // arena: tw_x (twx entries), ex (nx) | tw_y (twy), ey (ny) | ylim, xi (nx int) | xf (nx) | yi (ny) | yf (ny)
+  const bool stage_tw = fast && RS_TW_STAGE_MAJOR;
+  const size_t twx = stage_tw ? std::max(stage_twiddle_len(nx), 1) : nx;
+  const size_t twy = stage_tw ? std::max(stage_twiddle_len(ny), 1) : ny;
+  const size_t bytes = align8(sizeof(float2) * (twx + nx)) + align8(sizeof(float2) * (twy + ny)) +
                        align8(sizeof(int) * 2 * nx) + align8(sizeof(float) * nx) +
                        align8(sizeof(int) * ny) + align8(sizeof(float) * ny);
   e = cudaMalloc(&p->arena, bytes);
   if (e != cudaSuccess) { delete p; return fail(RS_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
   char* c = static_cast<char*>(p->arena);
-  p->tw_x = reinterpret_cast<float2*>(c); c += align8(sizeof(float2) * nx);
-  p->ex = reinterpret_cast<float2*>(c); c += align8(sizeof(float2) * nx);
-  p->tw_y = reinterpret_cast<float2*>(c); c += align8(sizeof(float2) * ny);
-  p->ey = reinterpret_cast<float2*>(c); c += align8(sizeof(float2) * ny);
+  p->tw_x = reinterpret_cast<float2*>(c);
+  p->ex = p->tw_x + twx;
+  c += align8(sizeof(float2) * (twx + nx));
+  p->tw_y = reinterpret_cast<float2*>(c);
+  p->ey = p->tw_y + twy;
+  c += align8(sizeof(float2) * (twy + ny));
   p->ylim = reinterpret_cast<int*>(c); c += align8(sizeof(int) * nx);
   p->xi = reinterpret_cast<int*>(c); c += align8(sizeof(int) * nx);
   p->xf = reinterpret_cast<float*>(c); c += align8(sizeof(float) * nx);
   p->yi = reinterpret_cast<int*>(c); c += align8(sizeof(int) * ny);
   p->yf = reinterpret_cast<float*>(c);
-  e = launch_twiddles(p->tw_x, nx, 0);
-  if (e == cudaSuccess) e = launch_twiddles(p->tw_y, ny, 0);
+  e = stage_tw ? launch_stage_twiddles(nx, p->tw_x, 0) : launch_twiddles(p->tw_x, nx, 0);
+  if (e == cudaSuccess) e = stage_tw ? launch_stage_twiddles(ny, p->tw_y, 0) : launch_twiddles(p->tw_y, ny, 0);
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   if (e != cudaSuccess) {
     cudaFree(p->arena);

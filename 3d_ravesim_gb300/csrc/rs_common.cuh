@@ -9,9 +9,22 @@
 
 namespace rs {
 
+// Blackwell (sm_100+) executes two FP32 adds / multiplies of a register pair in one
+// instruction; complex add, subtract and real scaling map onto them one to one, which halves
+// the instruction count of the DFT butterflies. RS_PACKED_F32X2=0 selects scalar arithmetic
+// (same rounding: each lane is an IEEE round-to-nearest add or multiply either way).
+#ifndef RS_PACKED_F32X2
+#define RS_PACKED_F32X2 1
+#endif
+#if RS_PACKED_F32X2 && defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return __fmul2_rn(a, make_float2(s, s)); }
+#else
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+#endif
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
@@ -114,10 +127,25 @@ __device__ __forceinline__ void dft16(float2 (&a)[16]) {
   for (int k = 0; k < 16; ++k) a[k] = y[k];
 }
 
-// Radix-R DFT on the R registers v[OFF .. OFF+R-1] of a 16-register array.
-template <int R, bool INV, int OFF>
-__device__ __forceinline__ void dft_slice(float2 (&v)[16]) {
+// 3-point DFT: y0 = a0 + t, y1,2 = a0 - t/2 -+ i*(sqrt(3)/2)*(a1 - a2) (forward), t = a1 + a2.
+constexpr float kHalfSqrt3 = 0.86602540378443864676f;
+
+template <bool INV>
+__device__ __forceinline__ void dft3(float2& a0, float2& a1, float2& a2) {
+  const float2 t = cadd(a1, a2);
+  const float2 d = csub(a1, a2);
+  const float2 m = make_float2(fmaf(-0.5f, t.x, a0.x), fmaf(-0.5f, t.y, a0.y));
+  const float2 q = cscale(mul_mi<INV>(d), kHalfSqrt3);
+  a0 = cadd(a0, t);
+  a1 = cadd(m, q);
+  a2 = csub(m, q);
+}
+
+// Radix-R DFT on the R registers v[OFF .. OFF+R-1] of an E-register array.
+template <int R, bool INV, int OFF, int E>
+__device__ __forceinline__ void dft_slice(float2 (&v)[E]) {
   if constexpr (R == 16) {
+    static_assert(E == 16 && OFF == 0, "radix-16 stages use the whole 16-register array");
     dft16<INV>(v);
   } else if constexpr (R == 8) {
     float2 a[8];
@@ -128,6 +156,8 @@ __device__ __forceinline__ void dft_slice(float2 (&v)[16]) {
     for (int i = 0; i < 8; ++i) v[OFF + i] = a[i];
   } else if constexpr (R == 4) {
     dft4<INV>(v[OFF], v[OFF + 1], v[OFF + 2], v[OFF + 3]);
+  } else if constexpr (R == 3) {
+    dft3<INV>(v[OFF], v[OFF + 1], v[OFF + 2]);
   } else if constexpr (R == 2) {
     dft2<INV>(v[OFF], v[OFF + 1]);
   }

@@ -1,0 +1,28 @@
+// rs_dispatch.cu — size dispatch of the fused passes over the two size families.
+#include "rs_passes.cuh"
+
+namespace rs {
+
+static bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+bool fast_size(int n) {
+  if (n < 16) return false;
+  if (is_pow2(n)) return n <= 16384;
+  return n % 3 == 0 && is_pow2(n / 3) && n >= 24 && n <= 12288;
+}
+
+cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s) {
+  return is_pow2(nx) ? launch_row_pass_pow2(nx, a, s) : launch_row_pass_pow3(nx, a, s);
+}
+
+cudaError_t launch_col_pass(int ny, const ColArgs& a, cudaStream_t s) {
+  return is_pow2(ny) ? launch_col_pass_pow2(ny, a, s) : launch_col_pass_pow3(ny, a, s);
+}
+
+cudaError_t launch_stage_twiddles(int n, float2* tw, cudaStream_t s) {
+  return is_pow2(n) ? launch_stage_twiddles_pow2(n, tw, s) : launch_stage_twiddles_pow3(n, tw, s);
+}
+
+int stage_twiddle_len(int n) { return is_pow2(n) ? stage_twiddle_len_pow2(n) : stage_twiddle_len_pow3(n); }
+
+}  // namespace rs

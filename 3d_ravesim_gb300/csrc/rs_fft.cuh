@@ -1,7 +1,8 @@
-// rs_fft.cuh — register-resident Stockham FFT for power-of-two lengths 16..16384.
+// rs_fft.cuh — register-resident Stockham FFT for lengths 2^k and 3*2^k (16..16384).
 //
-// Each sequence of length N is processed by T = N/16 threads that each hold 16 complex
-// values in registers. A stage of radix R performs 16/R butterflies per thread; between
+// Each sequence of length N is processed by T = N/E threads that each hold E complex values
+// in registers (E = 16, or 24 for 3*2^k). A stage of radix R performs E/R butterflies per
+// thread; between
 // stages the values go through a padded shared-memory buffer (one float2 pad per 16
 // elements, which makes the stride-16 writes of the first stage bank-conflict free).
 //
@@ -20,24 +21,47 @@
 #include <utility>
 #include "rs_common.cuh"
 
+#ifndef RS_TW_STAGE_MAJOR
+#define RS_TW_STAGE_MAJOR 1
+#endif
+
 namespace rs {
 
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
 template <int N>
 struct FftPlan {
-  static_assert(N >= 16 && (N & (N - 1)) == 0, "power-of-two length >= 16");
-  static constexpr int LG = ilog2c(N);
-  static constexpr int NFULL = LG / 4;                 // radix-16 stages
-  static constexpr int REM = 1 << (LG % 4);            // trailing radix (1 = none)
-  static constexpr int NST = NFULL + (REM > 1 ? 1 : 0);
-  static constexpr int T = N / 16;                     // threads per sequence
-  static constexpr int S = N + N / 16;                 // padded shared buffer length
-  __host__ __device__ static constexpr int radix(bool inv, int s) {
-    return ((inv ? (NST - 1 - s) : s) < NFULL) ? 16 : REM;
+  // Power-of-two lengths: 16 values per thread, radix-16 stages plus one radix-2/4/8 stage.
+  // Lengths 3*2^k: 24 values per thread, radix-8 stages, one radix-2/4 stage, one radix-3 stage.
+  static constexpr bool POW2 = (N & (N - 1)) == 0;
+  static constexpr int M = POW2 ? N : N / 3;
+  static_assert((M & (M - 1)) == 0 && (POW2 || M * 3 == N), "N must be 2^k or 3*2^k");
+  static_assert(N >= 16, "N >= 16");
+  static constexpr int LG = ilog2c(M);
+  static constexpr int BIG = POW2 ? 16 : 8;
+  static constexpr int LB = POW2 ? 4 : 3;
+  static constexpr int NBIG = LG / LB;
+  static constexpr int REM = 1 << (LG % LB);
+  static constexpr int NST = NBIG + (REM > 1 ? 1 : 0) + (POW2 ? 0 : 1);
+  static constexpr int E = POW2 ? 16 : 24;       // values per thread
+  static constexpr int T = N / E;                // threads per sequence
+  static constexpr int S = N + N / 16;           // padded shared buffer length
+  __host__ __device__ static constexpr int fwd_radix(int s) {
+    return s < NBIG ? BIG : ((s == NBIG && REM > 1) ? REM : 3);
   }
+  __host__ __device__ static constexpr int radix(bool inv, int s) { return fwd_radix(inv ? (NST - 1 - s) : s); }
   __host__ __device__ static constexpr int entry_radix(bool inv) { return radix(inv, 0); }
   __host__ __device__ static constexpr int exit_radix(bool inv) { return radix(inv, NST - 1); }
+  // Ns (product of the radices before stage s) in the given direction.
+  __host__ __device__ static constexpr int ns(bool inv, int s) { return s == 0 ? 1 : ns(inv, s - 1) * radix(inv, s - 1); }
+  // Stage-major twiddle table: stage s (Ns > 1) holds W_N^{r*k*N/(Ns*R)} at
+  // stage_offset(s) + (r-1)*Ns + k, so consecutive k (consecutive lanes) read consecutive
+  // entries. The forward table comes first, the inverse one (conjugated on use) at N_TW.
+  __host__ __device__ static constexpr int stage_offset(bool inv, int s) {
+    return s <= 1 ? 0 : stage_offset(inv, s - 1) + (radix(inv, s - 1) - 1) * ns(inv, s - 1);
+  }
+  __host__ __device__ static constexpr int table_len(bool inv) { return stage_offset(inv, NST); }
+  static constexpr int N_TW = table_len(false);
 };
 
 __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
@@ -45,47 +69,57 @@ __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
 // Position held by register e of thread t in a radix-R mapping.
 template <int N, int R>
 __device__ __forceinline__ int slot_pos(int t, int e) {
-  return t + (e / R) * (N / 16) + (e % R) * (N / R);
+  return t + (e / R) * FftPlan<N>::T + (e % R) * (N / R);
 }
 
-template <int R, bool INV, int... Bs>
-__device__ __forceinline__ void dft_all(float2 (&v)[16], std::integer_sequence<int, Bs...>) {
-  (dft_slice<R, INV, Bs * R>(v), ...);
+template <int R, bool INV, int E, int... Bs>
+__device__ __forceinline__ void dft_all(float2 (&v)[E], std::integer_sequence<int, Bs...>) {
+  (dft_slice<R, INV, Bs * R, E>(v), ...);
 }
 
 template <int N, bool INV, int SI, int NS>
 struct FftStages {
-  static __device__ __forceinline__ void run(float2 (&v)[16], float2* buf, int t,
+  using P = FftPlan<N>;
+  static __device__ __forceinline__ void run(float2 (&v)[P::E], float2* buf, int t,
                                              const float2* __restrict__ tw) {
-    using P = FftPlan<N>;
+    constexpr int E = P::E;
     constexpr int R = P::radix(INV, SI);
-    constexpr int B = 16 / R;
+    constexpr int B = E / R;
     constexpr int T = P::T;
     if constexpr (NS > 1) {
 #pragma unroll
       for (int b = 0; b < B; ++b) {
-        const int k = (t + b * T) & (NS - 1);
+        const int k = (t + b * T) % NS;
+#if RS_TW_STAGE_MAJOR
+        constexpr int TW_OFF = (INV ? P::N_TW : 0) + P::stage_offset(INV, SI);
+        const float2* tws = tw + TW_OFF + k;
+#else
         const int step = k * (N / (NS * R));
+#endif
 #pragma unroll
         for (int r = 1; r < R; ++r) {
+#if RS_TW_STAGE_MAJOR
+          const float2 w = __ldg(&tws[(r - 1) * NS]);
+#else
           const float2 w = __ldg(&tw[r * step]);
+#endif
           v[b * R + r] = INV ? cmulc(v[b * R + r], w) : cmul(v[b * R + r], w);
         }
       }
     }
-    dft_all<R, INV>(v, std::make_integer_sequence<int, B>{});
+    dft_all<R, INV, E>(v, std::make_integer_sequence<int, B>{});
     if constexpr (SI + 1 < P::NST) {
       constexpr int R2 = P::radix(INV, SI + 1);
 #pragma unroll
       for (int b = 0; b < B; ++b) {
         const int j = t + b * T;
-        const int base = (j / NS) * NS * R + (j & (NS - 1));
+        const int base = (j / NS) * NS * R + (j % NS);
 #pragma unroll
         for (int q = 0; q < R; ++q) buf[padi(base + q * NS)] = v[b * R + q];
       }
       __syncthreads();
 #pragma unroll
-      for (int e = 0; e < 16; ++e) v[e] = buf[padi(slot_pos<N, R2>(t, e))];
+      for (int e = 0; e < E; ++e) v[e] = buf[padi(slot_pos<N, R2>(t, e))];
       __syncthreads();
       FftStages<N, INV, SI + 1, NS * R>::run(v, buf, t, tw);
     }
@@ -94,9 +128,9 @@ struct FftStages {
 
 // Full transform of one sequence. On entry v is in the entry mapping of this direction,
 // on exit in its exit mapping. Every thread of the block must call it (it synchronises).
-// tw[m] = exp(-2*pi*i*m/N), m in [0, N).
+// tw: the stage-major tables (RS_TW_STAGE_MAJOR) or tw[m] = exp(-2*pi*i*m/N), m in [0, N).
 template <int N, bool INV>
-__device__ __forceinline__ void fft_seq(float2 (&v)[16], float2* buf, int t,
+__device__ __forceinline__ void fft_seq(float2 (&v)[FftPlan<N>::E], float2* buf, int t,
                                         const float2* __restrict__ tw) {
   FftStages<N, INV, 0, 1>::run(v, buf, t, tw);
 }

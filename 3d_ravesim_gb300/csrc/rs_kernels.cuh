@@ -134,6 +134,17 @@ __device__ __forceinline__ float2 voxel_db(const VoxelArgs& p, int xi, float fx,
   return make_float2(y0.x * (1.0f - fy) + y1.x * fy, y0.y * (1.0f - fy) + y1.y * fy);
 }
 
+__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float f) {
+  return make_float2(a.x * (1.0f - f) + b.x * f, a.y * (1.0f - f) + b.y * f);
+}
+
+// Voxel column j of grid row yi blended in y with weight fy (zero-weight rows are not read).
+__device__ __forceinline__ float2 voxel_col_blend(const VoxelArgs& p, int j, int yi, float fy) {
+  const float2 d0 = db_lookup(p, p.slice, yi * p.nxv + j);
+  if (fy == 0.0f) return d0;
+  return lerp2(d0, db_lookup(p, p.slice, (yi + 1) * p.nxv + j), fy);
+}
+
 __device__ __forceinline__ double plasma_load(const void* g, int f64, int lin) {
   return f64 ? __ldg(static_cast<const double*>(g) + lin)
              : static_cast<double>(__ldg(static_cast<const float*>(g) + lin));
@@ -174,6 +185,12 @@ __device__ __forceinline__ float2 plasma_db(const PlasmaArgs& p, int xi, float f
   return make_float2(y0.x * (1.0f - fy) + y1.x * fy, y0.y * (1.0f - fy) + y1.y * fy);
 }
 
+__device__ __forceinline__ float2 plasma_col_blend(const PlasmaArgs& p, int j, int yi, float fy) {
+  const float2 d0 = plasma_db_voxel(p, yi * p.nxv + j);
+  if (fy == 0.0f) return d0;
+  return lerp2(d0, plasma_db_voxel(p, (yi + 1) * p.nxv + j), fy);
+}
+
 // 1/(2*pi) as a double-double (hi + lo), for reducing the FP64 phase r*(2*pi/wl) to cycles.
 constexpr double kInv2PiHi = 0.15915494309189535;
 constexpr double kInv2PiLo = -9.839338337591243e-18;
@@ -199,7 +216,7 @@ __device__ __forceinline__ float2 point_source_value(const PointSrcArgs& p, int 
 
 // ----------------------------------------------------------------------------- row pass
 template <int N, int ROWS>
-__global__ void __launch_bounds__(ROWS * (N / 16)) row_pass_kernel(const RowArgs a) {
+__global__ void __launch_bounds__(ROWS * FftPlan<N>::T) row_pass_kernel(const RowArgs a) {
   using P = FftPlan<N>;
   constexpr int T = P::T;
   constexpr int RF = P::entry_radix(false);   // forward entry == inverse exit mapping
@@ -212,60 +229,75 @@ __global__ void __launch_bounds__(ROWS * (N / 16)) row_pass_kernel(const RowArgs
   float2* buf = smem + lr * P::S;
   const size_t rbase = static_cast<size_t>(valid ? row : 0) * N;
   const int flags = a.flags;
-  float2 v[16];
+  constexpr int E = P::E;
+  float2 v[E];
 
   if (flags & ROW_INV) {
 #pragma unroll
-    for (int e = 0; e < 16; ++e)
+    for (int e = 0; e < E; ++e)
       v[e] = valid ? a.in[rbase + slot_pos<N, RX>(t, e)] : make_float2(0.f, 0.f);
     fft_seq<N, true>(v, buf, t, a.tw);
   } else if (flags & ROW_SRC) {
 #pragma unroll
-    for (int e = 0; e < 16; ++e) v[e] = point_source_value(a.ps, slot_pos<N, RF>(t, e), row);
+    for (int e = 0; e < E; ++e) v[e] = point_source_value(a.ps, slot_pos<N, RF>(t, e), row);
   } else {
 #pragma unroll
-    for (int e = 0; e < 16; ++e)
+    for (int e = 0; e < E; ++e)
       v[e] = valid ? a.in[rbase + slot_pos<N, RF>(t, e)] : make_float2(0.f, 0.f);
   }
 
-  if ((flags & (ROW_TVOX | ROW_TPLASMA)) && valid) {
-    const int yi = __ldg(&a.ax.yi[row]);
+  if (flags & (ROW_TVOX | ROW_TPLASMA)) {
+    // The exchange buffer is idle between the two transforms: stage the voxel row blended in y
+    // there (one gather per voxel column instead of four per pixel), then interpolate in x.
+    const bool vox = flags & ROW_TVOX;
+    const int nxv = vox ? a.vox.nxv : a.pl.nxv;
+    const bool staged = nxv <= P::S;  // uniform across the block
+    int yi = -1;
+    float fy = 0.0f;
+    if (valid) {
+      yi = __ldg(&a.ax.yi[row]);
+      if (yi >= 0) fy = __ldg(&a.ax.yf[row]);
+    }
+    if (staged) {
+      if (yi >= 0) {
+        for (int j = t; j < nxv; j += T) buf[j] = vox ? voxel_col_blend(a.vox, j, yi, fy) : plasma_col_blend(a.pl, j, yi, fy);
+      }
+      __syncthreads();
+    }
     if (yi >= 0) {
-      const float fy = __ldg(&a.ax.yf[row]);
 #pragma unroll
-      for (int e = 0; e < 16; ++e) {
+      for (int e = 0; e < E; ++e) {
         const int x = slot_pos<N, RF>(t, e);
         const int xi = __ldg(&a.ax.xi[x]);
         if (xi >= 0) {
           const float fx = __ldg(&a.ax.xf[x]);
-          float2 tr;
-          if (flags & ROW_TVOX) {
-            const float2 d = voxel_db(a.vox, xi, fx, yi, fy);
-            if (d.x == 0.0f && d.y == 0.0f) continue;  // vacuum: factor exactly 1
-            tr = material_factor(d.x, d.y, a.vox.a);
+          float2 d;
+          if (staged) {
+            d = buf[xi];
+            if (fx != 0.0f) d = lerp2(d, buf[xi + 1], fx);
           } else {
-            const float2 d = plasma_db(a.pl, xi, fx, yi, fy);
-            if (d.x == 0.0f && d.y == 0.0f) continue;
-            tr = material_factor(d.x, d.y, a.pl.a);
+            d = vox ? voxel_db(a.vox, xi, fx, yi, fy) : plasma_db(a.pl, xi, fx, yi, fy);
           }
-          v[e] = cmul(v[e], tr);
+          if (d.x == 0.0f && d.y == 0.0f) continue;  // vacuum: factor exactly 1
+          v[e] = cmul(v[e], material_factor(d.x, d.y, vox ? a.vox.a : a.pl.a));
         }
       }
     }
+    if (staged) __syncthreads();  // the forward transform reuses the buffer
   }
 
   if (flags & ROW_FWD) {
     fft_seq<N, false>(v, buf, t, a.tw);
     if (valid) {
 #pragma unroll
-      for (int e = 0; e < 16; ++e) {
+      for (int e = 0; e < E; ++e) {
         const float2 o = (flags & ROW_SCALE) ? cscale(v[e], a.scale) : v[e];
         a.out[rbase + slot_pos<N, RX>(t, e)] = o;
       }
     }
   } else if (valid) {
 #pragma unroll
-    for (int e = 0; e < 16; ++e) {
+    for (int e = 0; e < E; ++e) {
       const float2 o = (flags & ROW_SCALE) ? cscale(v[e], a.scale) : v[e];
       a.out[rbase + slot_pos<N, RF>(t, e)] = o;
     }
@@ -278,31 +310,34 @@ __global__ void __launch_bounds__(ROWS * (N / 16)) row_pass_kernel(const RowArgs
 template <int N, int W>
 struct ColGeom {
   static constexpr int SC = FftPlan<N>::S + 16 / W;
-  static constexpr int THREADS = W * (N / 16);
+  static constexpr int THREADS = W * FftPlan<N>::T;
   static constexpr size_t SMEM = static_cast<size_t>(W) * SC * sizeof(float2);
 };
 
 template <int N, int W>
-__global__ void __launch_bounds__(W * (N / 16)) col_pass_kernel(const ColArgs a) {
+__global__ void __launch_bounds__(W * FftPlan<N>::T) col_pass_kernel(const ColArgs a) {
   using P = FftPlan<N>;
   constexpr int RF = P::entry_radix(false);
   constexpr int RX = P::exit_radix(false);
   extern __shared__ float2 smem[];
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
-  const int x = blockIdx.x * W + c;
-  float2* buf = smem + c * ColGeom<N, W>::SC;
   const int nx = a.nx;
+  // the last strip may be partial; its idle columns still take part in the block barriers
+  const bool live = blockIdx.x * W + c < nx;
+  const int x = live ? blockIdx.x * W + c : nx - 1;
+  float2* buf = smem + c * ColGeom<N, W>::SC;
   const int flags = a.flags;
-  float2 v[16];
+  constexpr int E = P::E;
+  float2 v[E];
 
   if (flags & COL_FWD) {
 #pragma unroll
-    for (int e = 0; e < 16; ++e) v[e] = a.in[static_cast<size_t>(slot_pos<N, RF>(t, e)) * nx + x];
+    for (int e = 0; e < E; ++e) v[e] = a.in[static_cast<size_t>(slot_pos<N, RF>(t, e)) * nx + x];
     fft_seq<N, false>(v, buf, t, a.tw);
   } else {
 #pragma unroll
-    for (int e = 0; e < 16; ++e) v[e] = a.in[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x];
+    for (int e = 0; e < E; ++e) v[e] = a.in[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x];
   }
 
   // registers are in the forward-exit (== inverse-entry) mapping: position = fy
@@ -310,7 +345,7 @@ __global__ void __launch_bounds__(W * (N / 16)) col_pass_kernel(const ColArgs a)
     const int lim = __ldg(&a.ylim[x]);
     const float2 exv = (flags & COL_H) ? __ldg(&a.ex[x]) : make_float2(1.f, 0.f);
 #pragma unroll
-    for (int e = 0; e < 16; ++e) {
+    for (int e = 0; e < E; ++e) {
       const int fy = slot_pos<N, RX>(t, e);
       const int m = fy < (N + 1) / 2 ? fy : fy - N;
       const bool keep = (m < 0 ? -m : m) <= lim;
@@ -321,21 +356,23 @@ __global__ void __launch_bounds__(W * (N / 16)) col_pass_kernel(const ColArgs a)
       }
     }
   }
-  if (flags & COL_SPEC) {
+  if ((flags & COL_SPEC) && live) {
 #pragma unroll
-    for (int e = 0; e < 16; ++e) a.spec[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x] = v[e];
+    for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x] = v[e];
   }
   if (flags & COL_SCALE) {
 #pragma unroll
-    for (int e = 0; e < 16; ++e) v[e] = cscale(v[e], a.scale);
+    for (int e = 0; e < E; ++e) v[e] = cscale(v[e], a.scale);
   }
   if (flags & COL_INV) {
     fft_seq<N, true>(v, buf, t, a.tw);
+    if (live) {
 #pragma unroll
-    for (int e = 0; e < 16; ++e) a.out[static_cast<size_t>(slot_pos<N, RF>(t, e)) * nx + x] = v[e];
-  } else {
+      for (int e = 0; e < E; ++e) a.out[static_cast<size_t>(slot_pos<N, RF>(t, e)) * nx + x] = v[e];
+    }
+  } else if (live) {
 #pragma unroll
-    for (int e = 0; e < 16; ++e) a.out[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x] = v[e];
+    for (int e = 0; e < E; ++e) a.out[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x] = v[e];
   }
 }
 
@@ -345,8 +382,11 @@ __global__ void __launch_bounds__(W * (N / 16)) col_pass_kernel(const ColArgs a)
 void note_launch(unsigned n = 1);
 
 cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s);
+// Twiddles used by the fused passes of length n (fast sizes only): stage-major tables, or the
+// plain table tw[m] = exp(-2*pi*i*m/n) when RS_TW_STAGE_MAJOR is 0.
+cudaError_t launch_stage_twiddles(int n, float2* tw, cudaStream_t s);
+int stage_twiddle_len(int n);
 cudaError_t launch_col_pass(int ny, const ColArgs& a, cudaStream_t s);
-int col_strip_width(int ny);
 bool fast_size(int n);
 
 }  // namespace rs

@@ -1,0 +1,117 @@
+// rs_passes.cuh — launch templates of the fused row / column passes and of the stage-major
+// twiddle tables. rs_pass_pow2.cu and rs_pass_pow3.cu instantiate them for the two size
+// families (2^k and 3*2^k) in separate translation units that compile in parallel.
+#pragma once
+#include "rs_kernels.cuh"
+
+namespace rs {
+
+// Rows per block: one row when a row has >= 256 threads, otherwise enough rows for ~256 threads.
+template <int N>
+constexpr int rows_per_block() {
+  return FftPlan<N>::T >= 256 ? 1 : 256 / FftPlan<N>::T;
+}
+
+template <int N>
+cudaError_t launch_rows_n(const RowArgs& a, cudaStream_t s) {
+  constexpr int ROWS = rows_per_block<N>();
+  constexpr int THREADS = ROWS * FftPlan<N>::T;
+  constexpr size_t SMEM = static_cast<size_t>(ROWS) * FftPlan<N>::S * sizeof(float2);
+  static unsigned configured = 0;  // one bit per device ordinal
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+  const unsigned bit = 1u << (dev & 31);
+  if (!(configured & bit)) {
+    cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<N, ROWS>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(SMEM));
+    if (e != cudaSuccess) return e;
+    configured |= bit;
+  }
+  const int blocks = (a.ny + ROWS - 1) / ROWS;
+  row_pass_kernel<N, ROWS><<<blocks, THREADS, SMEM, s>>>(a);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) note_launch();
+  return e;
+}
+
+// Stage-major twiddle tables (forward plan, then inverse plan) in FP64, rounded to float.
+template <int N>
+__global__ void stage_twiddles_kernel(float2* tw) {
+  using P = FftPlan<N>;
+  constexpr int NF = P::table_len(false);
+  constexpr int NI = P::table_len(true);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= NF + NI) return;
+  const bool inv = i >= NF;
+  const int j = inv ? i - NF : i;
+  int s = 1;
+  while (s + 1 < P::NST && P::stage_offset(inv, s + 1) <= j) ++s;
+  const int ns = P::ns(inv, s);
+  const int r = (j - P::stage_offset(inv, s)) / ns + 1;
+  const int k = (j - P::stage_offset(inv, s)) % ns;
+  const long long m = static_cast<long long>(r) * k * (N / (ns * P::radix(inv, s)));
+  double sn, cs;
+  sincospi(-2.0 * static_cast<double>(m) / static_cast<double>(N), &sn, &cs);
+  tw[i] = make_float2(static_cast<float>(cs), static_cast<float>(sn));
+}
+
+template <int N>
+cudaError_t launch_stage_twiddles_n(float2* tw, cudaStream_t s) {
+  constexpr int total = FftPlan<N>::table_len(false) + FftPlan<N>::table_len(true);
+  if (total == 0) return cudaSuccess;
+  stage_twiddles_kernel<N><<<(total + 255) / 256, 256, 0, s>>>(tw);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) note_launch();
+  return e;
+}
+
+template <int N>
+constexpr int stage_twiddle_len_n() { return FftPlan<N>::table_len(false) + FftPlan<N>::table_len(true); }
+
+
+// Columns per block: W*T threads (T = threads per column), capped at 512 threads so that the
+// 16 or 24 complex values each thread keeps in registers fit without spilling, and W <= 16.
+template <int N>
+constexpr int strip_width() {
+  constexpr int t = FftPlan<N>::T;
+  constexpr int w = t >= 512 ? 1 : 512 / t;
+  return w > 16 ? 16 : w;
+}
+
+template <int N, int W>
+cudaError_t launch_cols_nw(const ColArgs& a, cudaStream_t s) {
+  using G = ColGeom<N, W>;
+  static unsigned configured = 0;  // one bit per device ordinal
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+  const unsigned bit = 1u << (dev & 31);
+  if (!(configured & bit)) {
+    cudaError_t e = cudaFuncSetAttribute(col_pass_kernel<N, W>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(G::SMEM));
+    if (e != cudaSuccess) return e;
+    configured |= bit;
+  }
+  col_pass_kernel<N, W><<<(a.nx + W - 1) / W, G::THREADS, G::SMEM, s>>>(a);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) note_launch();
+  return e;
+}
+
+
+#define RS_POW2_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192) X(16384)
+#define RS_POW3_SIZES(X) X(24) X(48) X(96) X(192) X(384) X(768) X(1536) X(3072) X(6144) X(12288)
+
+// Per-family dispatchers (rs_pass_pow2.cu / rs_pass_pow3.cu); return cudaErrorInvalidValue
+// for a size outside the family.
+cudaError_t launch_row_pass_pow2(int n, const RowArgs& a, cudaStream_t s);
+cudaError_t launch_row_pass_pow3(int n, const RowArgs& a, cudaStream_t s);
+cudaError_t launch_col_pass_pow2(int n, const ColArgs& a, cudaStream_t s);
+cudaError_t launch_col_pass_pow3(int n, const ColArgs& a, cudaStream_t s);
+cudaError_t launch_stage_twiddles_pow2(int n, float2* tw, cudaStream_t s);
+cudaError_t launch_stage_twiddles_pow3(int n, float2* tw, cudaStream_t s);
+int stage_twiddle_len_pow2(int n);
+int stage_twiddle_len_pow3(int n);
+
+}  // namespace rs

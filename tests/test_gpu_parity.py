@@ -23,7 +23,8 @@ def host(v, ny, nx):
     return v.to_numpy().reshape(ny, nx)
 
 
-FAST = [(16, 16), (32, 64), (64, 32), (128, 256), (512, 128), (1024, 64), (256, 2048), (4096, 16), (64, 4096)]
+FAST = [(16, 16), (32, 64), (64, 32), (128, 256), (512, 128), (1024, 64), (256, 2048), (4096, 16), (64, 4096),
+        (24, 48), (96, 1536), (3072, 64), (1536, 192), (768, 384), (48, 6144), (12288, 16)]
 GENERIC = [(40, 28), (72, 72), (24, 16), (48, 64), (3, 3), (4, 4)]
 
 
@@ -106,7 +107,8 @@ def test_propagate_2d_vs_golden_generic_size(rs, cuda, golden):
         assert rel_l2(host(U, ny, nx), golden[f"prop_{name}_skip_U"]) < 1e-5
 
 
-@pytest.mark.parametrize("nx,ny", [(64, 64), (128, 512), (1024, 1024), (256, 4096)])
+@pytest.mark.parametrize("nx,ny", [(64, 64), (128, 512), (1024, 1024), (256, 4096), (1536, 1536), (3072, 96),
+                                   (24, 3072)])
 def test_propagate_2d_fast_sizes_vs_fp64_oracle(rs, cuda, oracle, nx, ny):
     rng = np.random.default_rng(nx + ny)
     x = (rng.normal(size=(ny, nx)) + 1j * rng.normal(size=(ny, nx)))
@@ -210,7 +212,7 @@ def test_sample_checkpoint_callback_path_matches_fused(rs, cuda, golden):
     assert rel_l2(host(u2, ny, nx), host(u1, ny, nx)) < 1e-6
 
 
-@pytest.mark.parametrize("nx,ny,nz", [(256, 256, 12), (512, 256, 5)])
+@pytest.mark.parametrize("nx,ny,nz", [(256, 256, 12), (512, 256, 5), (384, 192, 4)])
 def test_sample_fast_sizes_vs_fp64_oracle(rs, cuda, oracle, nx, ny, nz):
     """Shell sample with bilinear (non-aligned) voxels and aligned voxels, both fast-path sizes."""
     rng = np.random.default_rng(nx + nz)
@@ -309,3 +311,8 @@ def test_run_simulation_vs_golden(rs, cuda, golden):
     outs = ws.run_simulation(p, rs.PointSource(x=1e-6, y=0.0, z=0.0), [samp], [a0, a1], u, U, table)
     assert rel_l2(host(u, ny, nx), golden["run_u"]) < 2e-5
     assert rel_l2(outs[0], golden["run_out"]) < 2e-5
+
+
+def test_fast_plan_covers_both_size_families(rs, cuda):
+    for n, fast in ((4096, True), (3072, True), (1536, True), (24, True), (40, False), (72, False)):
+        assert rs._lib.plan_for(n, 64, cuda).fast is fast
