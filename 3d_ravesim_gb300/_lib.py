@@ -58,6 +58,8 @@ _SIGS = {
                               ctypes.POINTER(VoxelGeom), c_double, c_double, c_double, c_double,
                               _DP, _DP, c_int, c_int, _P], c_int),
     "rs_detector": ([_P, _P, _P, ctypes.POINTER(DetectorGeom), _P], c_int),
+    "rs_plan_set_pipeline": ([_P, c_int], c_int),
+    "rs_plan_status": ([_P, ctypes.POINTER(c_int)], c_int),
     "rs_launch_count": ([ctypes.POINTER(ctypes.c_ulonglong)], c_int),
     "rs_plan_profile": ([_P, c_int], c_int),
     "rs_plan_profile_read": ([_P, _DP, _DP, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),
@@ -130,6 +132,18 @@ class Plan:
         self.handle = handle
         self.fast = bool(lib().rs_plan_is_fast(handle))
         self._finalizer = weakref.finalize(self, Plan._destroy, handle, device)
+
+    def set_pipeline(self, enable: bool) -> None:
+        """Select the bulk-copy pipelined passes (default) or the classic per-block passes."""
+        with torch.cuda.device(self.device):
+            check(lib().rs_plan_set_pipeline(self.handle, 1 if enable else 0), "rs_plan_set_pipeline")
+
+    def status(self) -> int:
+        """Synchronise and return the device status word (0 = no bounded wait gave up)."""
+        st = c_int(0)
+        with torch.cuda.device(self.device):
+            check(lib().rs_plan_status(self.handle, ctypes.byref(st)), "rs_plan_status")
+        return st.value
 
     @staticmethod
     def _destroy(handle: c_void_p, device: torch.device) -> None:

@@ -9,12 +9,16 @@
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "rs_fresnel.h"
 #include "rs_misc.cuh"
+#include "rs_pipe_api.cuh"
 
 using namespace rs;
 
@@ -71,6 +75,15 @@ struct rs_plan {
   float* yf = nullptr;
   void* det = nullptr;
   size_t det_cap = 0;
+  // pipelined (bulk-copy) passes: enabled unless RS_PIPELINE=0 or rs_plan_set_pipeline(plan, 0)
+  bool pipe = true;
+  int* status = nullptr;  // device word set by bounded waits that gave up
+  struct MapEntry {
+    const void* ptr = nullptr;
+    CUtensorMap map;
+  };
+  MapEntry maps[4];
+  int map_next = 0;
   // optional per-pass event timing of the multislice loop (rs_plan_profile)
   bool prof = false;
   std::vector<cudaEvent_t> ev_pool;
@@ -124,6 +137,64 @@ int build_axes(rs_plan* p, const rs_voxel_geom* g, double dx, double dy, double 
 
 AxisTab axis_tab(const rs_plan* p) { return AxisTab{p->xi, p->xf, p->yi, p->yf}; }
 
+// ---- pipelined passes -------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
+
+bool tensor_map_encoder() {
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    cudaDriverEntryPointQueryResult q;
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      g_encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  return g_encode != nullptr;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// Tensor map of a (ny, nx) complex64 field viewed as 8-byte elements, box (w columns, bh rows).
+const CUtensorMap* field_map(rs_plan* p, const void* base, int w, int bh) {
+  for (auto& m : p->maps)
+    if (m.ptr == base) return &m.map;
+  auto& slot = p->maps[p->map_next];
+  p->map_next = (p->map_next + 1) % 4;
+  cuuint64_t dims[2] = {static_cast<cuuint64_t>(p->nx), static_cast<cuuint64_t>(p->ny)};
+  cuuint64_t strides[1] = {static_cast<cuuint64_t>(p->nx) * 8};
+  cuuint32_t box[2] = {static_cast<cuuint32_t>(w), static_cast<cuuint32_t>(bh)};
+  cuuint32_t es[2] = {1, 1};
+  const CUresult r = g_encode(&slot.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<void*>(base), dims, strides,
+                              box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    slot.ptr = nullptr;
+    return nullptr;
+  }
+  slot.ptr = base;
+  return &slot.map;
+}
+
+cudaError_t run_row(rs_plan* p, const RowArgs& r, cudaStream_t s) {
+  if (p->pipe && row_pipe_ok(p->nx) && (r.flags & ROW_SRC || aligned16(r.in)) && aligned16(r.out))
+    return launch_row_pipe(p->nx, r, p->status, s);
+  return launch_row_pass(p->nx, r, s);
+}
+
+cudaError_t run_col(rs_plan* p, const ColArgs& c, cudaStream_t s) {
+  int w = 0, bh = 0;
+  if (p->pipe && col_pipe_box(p->ny, &w, &bh) && aligned16(c.in) && aligned16(c.out) && tensor_map_encoder()) {
+    const CUtensorMap* mi = field_map(p, c.in, w, bh);
+    const CUtensorMap* mo = mi ? field_map(p, c.out, w, bh) : nullptr;
+    if (mi && mo) {
+      const CUtensorMap in_copy = *mi;  // field_map may recycle a slot; pass by value
+      return launch_col_pipe(p->ny, c, in_copy, *mo, p->status, s);
+    }
+  }
+  return launch_col_pass(p->ny, c, s);
+}
+
 // Records a start event before a pass when profiling is on; returns the pair index or -1.
 int prof_begin(rs_plan* p, int kind, cudaStream_t s) {
   if (!p->prof) return -1;
@@ -150,10 +221,10 @@ int fft2_impl(rs_plan* p, const float2* in, float2* out, cudaStream_t s) {
   if (p->fast) {
     RowArgs r{};
     r.in = in; r.out = out; r.ny = p->ny; r.flags = ROW_FWD; r.tw = p->tw_x;
-    RS_CK(launch_row_pass(p->nx, r, s));
+    RS_CK(run_row(p, r, s));
     ColArgs c{};
     c.in = out; c.out = out; c.nx = p->nx; c.flags = COL_FWD; c.tw = p->tw_y;
-    RS_CK(launch_col_pass(p->ny, c, s));
+    RS_CK(run_col(p, c, s));
   } else {
     RS_CK(launch_dft_axis(in, out, p->nx, p->ny, 0, 0, p->tw_x, 1.0f, s));
     RS_CK(launch_dft_axis(out, out, p->nx, p->ny, 1, 0, p->tw_y, 1.0f, s));
@@ -166,10 +237,10 @@ int ifft2_impl(rs_plan* p, const float2* in, float2* out, cudaStream_t s) {
   if (p->fast) {
     ColArgs c{};
     c.in = in; c.out = out; c.nx = p->nx; c.flags = COL_INV | COL_SCALE; c.scale = inv_n; c.tw = p->tw_y;
-    RS_CK(launch_col_pass(p->ny, c, s));
+    RS_CK(run_col(p, c, s));
     RowArgs r{};
     r.in = out; r.out = out; r.ny = p->ny; r.flags = ROW_INV; r.tw = p->tw_x;
-    RS_CK(launch_row_pass(p->nx, r, s));
+    RS_CK(run_row(p, r, s));
   } else {
     RS_CK(launch_dft_axis(in, out, p->nx, p->ny, 1, 1, p->tw_y, 1.0f, s));
     RS_CK(launch_dft_axis(out, out, p->nx, p->ny, 0, 1, p->tw_x, inv_n, s));
@@ -260,14 +331,14 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       r.vox = vox;
       r.pl = pl;
       const int er = prof_begin(p, 0, s);
-      RS_CK(launch_row_pass(p->nx, r, s));
+      RS_CK(run_row(p, r, s));
       prof_end(p, er, s);
       ColArgs c{};
       c.in = u; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_y;
       c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
       c.flags = COL_FWD | COL_H | COL_SCALE | COL_INV | (z == s1 - 1 ? COL_SPEC : 0);
       const int ec = prof_begin(p, 1, s);
-      RS_CK(launch_col_pass(p->ny, c, s));
+      RS_CK(run_col(p, c, s));
       prof_end(p, ec, s);
     } else {
       RS_TRY(generic_slice(p, u, U, src.plasma ? nullptr : &vox, src.plasma ? &pl : nullptr, s));
@@ -276,7 +347,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
   if (p->fast) {
     RowArgs r{};
     r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tw_x; r.flags = ROW_INV;
-    RS_CK(launch_row_pass(p->nx, r, s));
+    RS_CK(run_row(p, r, s));
   }
   return RS_OK;
 }
@@ -413,7 +484,7 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   const size_t twy = stage_tw ? std::max(stage_twiddle_len(ny), 1) : ny;
   const size_t bytes = align8(sizeof(float2) * (twx + nx)) + align8(sizeof(float2) * (twy + ny)) +
                        align8(sizeof(int) * 2 * nx) + align8(sizeof(float) * nx) +
-                       align8(sizeof(int) * ny) + align8(sizeof(float) * ny);
+                       align8(sizeof(int) * ny) + align8(sizeof(float) * ny) + 8;
   e = cudaMalloc(&p->arena, bytes);
   if (e != cudaSuccess) { delete p; return fail(RS_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
   char* c = static_cast<char*>(p->arena);
@@ -427,9 +498,13 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   p->xi = reinterpret_cast<int*>(c); c += align8(sizeof(int) * nx);
   p->xf = reinterpret_cast<float*>(c); c += align8(sizeof(float) * nx);
   p->yi = reinterpret_cast<int*>(c); c += align8(sizeof(int) * ny);
-  p->yf = reinterpret_cast<float*>(c);
+  p->yf = reinterpret_cast<float*>(c); c += align8(sizeof(float) * ny);
+  p->status = reinterpret_cast<int*>(c);
+  const char* env = std::getenv("RS_PIPELINE");
+  p->pipe = !(env && env[0] == '0');
   e = stage_tw ? launch_stage_twiddles(nx, p->tw_x, 0) : launch_twiddles(p->tw_x, nx, 0);
   if (e == cudaSuccess) e = stage_tw ? launch_stage_twiddles(ny, p->tw_y, 0) : launch_twiddles(p->tw_y, ny, 0);
+  if (e == cudaSuccess) e = cudaMemsetAsync(p->status, 0, sizeof(int), 0);
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   if (e != cudaSuccess) {
     cudaFree(p->arena);
@@ -455,6 +530,21 @@ int rs_plan_destroy(rs_plan* p) {
 }
 
 int rs_plan_is_fast(const rs_plan* p) { return p && p->fast ? 1 : 0; }
+
+int rs_plan_set_pipeline(rs_plan* p, int enable) {
+  RS_TRY(check_plan(p));
+  p->pipe = enable != 0;
+  return RS_OK;
+}
+
+int rs_plan_status(rs_plan* p, int* device_status) {
+  RS_TRY(check_plan(p));
+  if (!device_status) return fail(RS_EINVAL, "device_status is NULL");
+  RS_CK(cudaDeviceSynchronize());
+  RS_CK(cudaMemcpy(device_status, p->status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (*device_status != 0) return fail(RS_ETIMEOUT, "a pipelined pass gave up waiting for a bulk copy");
+  return RS_OK;
+}
 
 int rs_launch_count(unsigned long long* out) {
   if (!out) return fail(RS_EINVAL, "out is NULL");
@@ -530,16 +620,16 @@ int rs_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double wl
     if (!skip_fft) {
       RowArgs r{};
       r.in = u; r.out = U; r.ny = p->ny; r.flags = ROW_FWD; r.tw = p->tw_x;
-      RS_CK(launch_row_pass(p->nx, r, s));
+      RS_CK(run_row(p, r, s));
     }
     ColArgs c{};
     c.in = U; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_y;
     c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
     c.flags = (skip_fft ? 0 : COL_FWD) | COL_H | COL_SPEC | COL_SCALE | COL_INV;
-    RS_CK(launch_col_pass(p->ny, c, s));
+    RS_CK(run_col(p, c, s));
     RowArgs r{};
     r.in = u; r.out = u; r.ny = p->ny; r.flags = ROW_INV; r.tw = p->tw_x;
-    RS_CK(launch_row_pass(p->nx, r, s));
+    RS_CK(run_row(p, r, s));
   } else {
     if (!skip_fft) RS_TRY(fft2_impl(p, u, U, s));
     RS_CK(launch_transfer(U, p->nx, p->ny, p->ex, p->ey, p->ylim, 1, nullptr, s));
@@ -584,15 +674,15 @@ int rs_point_source_propagate(rs_plan* p, void* u_, void* U_, double dx, double 
   if (p->fast) {
     RowArgs r{};
     r.out = U; r.ny = p->ny; r.flags = ROW_SRC | ROW_FWD; r.tw = p->tw_x; r.ps = a;
-    RS_CK(launch_row_pass(p->nx, r, s));
+    RS_CK(run_row(p, r, s));
     ColArgs c{};
     c.in = U; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_y; c.ylim = p->ylim;
     c.scale = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
     c.flags = COL_FWD | COL_MASK | COL_SPEC | COL_SCALE | COL_INV;
-    RS_CK(launch_col_pass(p->ny, c, s));
+    RS_CK(run_col(p, c, s));
     RowArgs r2{};
     r2.in = u; r2.out = u; r2.ny = p->ny; r2.flags = ROW_INV; r2.tw = p->tw_x;
-    RS_CK(launch_row_pass(p->nx, r2, s));
+    RS_CK(run_row(p, r2, s));
   } else {
     RS_CK(launch_point_source(u, p->nx, p->ny, a, s));
     RS_TRY(fft2_impl(p, u, U, s));

@@ -25,4 +25,17 @@ cudaError_t launch_stage_twiddles(int n, float2* tw, cudaStream_t s) {
 
 int stage_twiddle_len(int n) { return is_pow2(n) ? stage_twiddle_len_pow2(n) : stage_twiddle_len_pow3(n); }
 
+bool row_pipe_ok(int n) { return is_pow2(n) ? row_pipe_ok_pow2(n) : row_pipe_ok_pow3(n); }
+bool col_pipe_box(int n, int* w, int* bh) { return is_pow2(n) ? col_pipe_box_pow2(n, w, bh) : col_pipe_box_pow3(n, w, bh); }
+
+cudaError_t launch_row_pipe(int nx, const RowArgs& a, int* status, cudaStream_t s) {
+  return is_pow2(nx) ? launch_row_pipe_pow2(nx, a, status, s) : launch_row_pipe_pow3(nx, a, status, s);
+}
+
+cudaError_t launch_col_pipe(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
+                            cudaStream_t s) {
+  return is_pow2(ny) ? launch_col_pipe_pow2(ny, a, in, out, status, s)
+                     : launch_col_pipe_pow3(ny, a, in, out, status, s);
+}
+
 }  // namespace rs

@@ -66,6 +66,17 @@ struct FftPlan {
 
 __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
 
+// Exchange-buffer addressing policies: element p of a sequence lives at AD::at(p) * STR.
+// PadAddr: one pad per 16 elements (buffers of FftPlan::S elements).
+// SwzAddr: XOR swizzle of p within its 16-element group (dense buffers of N elements, as
+// filled by bulk copies); conflict-free for all power-of-two exchange patterns.
+struct PadAddr {
+  static __device__ __forceinline__ int at(int p) { return padi(p); }
+};
+struct SwzAddr {
+  static __device__ __forceinline__ int at(int p) { return p ^ ((p >> 4) & 15); }
+};
+
 // Position held by register e of thread t in a radix-R mapping.
 template <int N, int R>
 __device__ __forceinline__ int slot_pos(int t, int e) {
@@ -77,7 +88,7 @@ __device__ __forceinline__ void dft_all(float2 (&v)[E], std::integer_sequence<in
   (dft_slice<R, INV, Bs * R, E>(v), ...);
 }
 
-template <int N, bool INV, int SI, int NS>
+template <int N, bool INV, int SI, int NS, class AD = PadAddr, int STR = 1>
 struct FftStages {
   using P = FftPlan<N>;
   static __device__ __forceinline__ void run(float2 (&v)[P::E], float2* buf, int t,
@@ -115,13 +126,13 @@ struct FftStages {
         const int j = t + b * T;
         const int base = (j / NS) * NS * R + (j % NS);
 #pragma unroll
-        for (int q = 0; q < R; ++q) buf[padi(base + q * NS)] = v[b * R + q];
+        for (int q = 0; q < R; ++q) buf[AD::at(base + q * NS) * STR] = v[b * R + q];
       }
       __syncthreads();
 #pragma unroll
-      for (int e = 0; e < E; ++e) v[e] = buf[padi(slot_pos<N, R2>(t, e))];
+      for (int e = 0; e < E; ++e) v[e] = buf[AD::at(slot_pos<N, R2>(t, e)) * STR];
       __syncthreads();
-      FftStages<N, INV, SI + 1, NS * R>::run(v, buf, t, tw);
+      FftStages<N, INV, SI + 1, NS * R, AD, STR>::run(v, buf, t, tw);
     }
   }
 };
@@ -129,10 +140,10 @@ struct FftStages {
 // Full transform of one sequence. On entry v is in the entry mapping of this direction,
 // on exit in its exit mapping. Every thread of the block must call it (it synchronises).
 // tw: the stage-major tables (RS_TW_STAGE_MAJOR) or tw[m] = exp(-2*pi*i*m/N), m in [0, N).
-template <int N, bool INV>
+template <int N, bool INV, class AD = PadAddr, int STR = 1>
 __device__ __forceinline__ void fft_seq(float2 (&v)[FftPlan<N>::E], float2* buf, int t,
                                         const float2* __restrict__ tw) {
-  FftStages<N, INV, 0, 1>::run(v, buf, t, tw);
+  FftStages<N, INV, 0, 1, AD, STR>::run(v, buf, t, tw);
 }
 
 }  // namespace rs

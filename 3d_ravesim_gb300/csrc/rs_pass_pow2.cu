@@ -40,4 +40,42 @@ int stage_twiddle_len_pow2(int n) {
   }
 }
 
+#define RS_ROWPIPE_CASE(N) \
+  case N: return launch_row_pipe_n<N>(a, status, s);
+#define RS_COLPIPE_CASE(N) \
+  case N: return launch_col_pipe_n<N>(a, in, out, status, s);
+#define RS_COLBOX_CASE(N) \
+  case N: *w = ColPipeGeom<N>::W; *bh = ColPipeGeom<N>::BH; return true;
+#define RS_ROWOK_CASE(N) \
+  case N: return true;
+
+cudaError_t launch_row_pipe_pow2(int n, const RowArgs& a, int* status, cudaStream_t s) {
+  switch (n) {
+    RS_POW2_PIPE_ROW(RS_ROWPIPE_CASE)
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+cudaError_t launch_col_pipe_pow2(int n, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out,
+                                 int* status, cudaStream_t s) {
+  switch (n) {
+    RS_POW2_PIPE_COL(RS_COLPIPE_CASE)
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+bool col_pipe_box_pow2(int n, int* w, int* bh) {
+  switch (n) {
+    RS_POW2_PIPE_COL(RS_COLBOX_CASE)
+    default: return false;
+  }
+}
+
+bool row_pipe_ok_pow2(int n) {
+  switch (n) {
+    RS_POW2_PIPE_ROW(RS_ROWOK_CASE)
+    default: return false;
+  }
+}
+
 }  // namespace rs

@@ -2,7 +2,7 @@
 // twiddle tables. rs_pass_pow2.cu and rs_pass_pow3.cu instantiate them for the two size
 // families (2^k and 3*2^k) in separate translation units that compile in parallel.
 #pragma once
-#include "rs_kernels.cuh"
+#include "rs_pipe.cuh"
 
 namespace rs {
 
@@ -99,6 +99,83 @@ cudaError_t launch_cols_nw(const ColArgs& a, cudaStream_t s) {
   return e;
 }
 
+
+// Persistent pipelined passes: one launch covers all tiles with (SMs x resident blocks) blocks.
+template <class K>
+int resident_grid(K kernel, int threads, size_t smem, int tiles) {
+  int dev = 0, sms = 1, per_sm = 1;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+  if (per_sm < 1) per_sm = 1;
+  return tiles < sms * per_sm ? tiles : sms * per_sm;
+}
+
+template <int N>
+cudaError_t launch_row_pipe_n(const RowArgs& a, int* status, cudaStream_t s) {
+  using G = RowPipeGeom<N>;
+  static unsigned configured = 0;
+  static int grid_cache[32];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+  const unsigned bit = 1u << (dev & 31);
+  if (!(configured & bit)) {
+    cudaError_t e = cudaFuncSetAttribute(row_pipe_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(G::SMEM));
+    if (e != cudaSuccess) return e;
+    grid_cache[dev & 31] = resident_grid(row_pipe_kernel<N>, G::THREADS, G::SMEM, 1 << 30);
+    configured |= bit;
+  }
+  const int tiles = (a.ny + G::RW - 1) / G::RW;
+  const int grid = tiles < grid_cache[dev & 31] ? tiles : grid_cache[dev & 31];
+  row_pipe_kernel<N><<<grid, G::THREADS, G::SMEM, s>>>(a, status);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) note_launch();
+  return e;
+}
+
+template <int N>
+cudaError_t launch_col_pipe_n(const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
+                              cudaStream_t s) {
+  using G = ColPipeGeom<N>;
+  static unsigned configured = 0;
+  static int grid_cache[32];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+  const unsigned bit = 1u << (dev & 31);
+  if (!(configured & bit)) {
+    cudaError_t e = cudaFuncSetAttribute(col_pipe_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(G::SMEM));
+    if (e != cudaSuccess) return e;
+    grid_cache[dev & 31] = resident_grid(col_pipe_kernel<N>, G::THREADS, G::SMEM, 1 << 30);
+    configured |= bit;
+  }
+  const int tiles = (a.nx + G::W - 1) / G::W;
+  const int grid = tiles < grid_cache[dev & 31] ? tiles : grid_cache[dev & 31];
+  col_pipe_kernel<N><<<grid, G::THREADS, G::SMEM, s>>>(a, in, out, status);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) note_launch();
+  return e;
+}
+
+// Sizes with a pipelined variant: rows need 3 tile buffers of >= 1 row; columns need strips of
+// >= 2 columns (16-byte tensor-copy boxes) with <= 512 threads.
+#define RS_POW2_PIPE_ROW(X) X(256) X(512) X(1024) X(2048) X(4096) X(8192)
+#define RS_POW2_PIPE_COL(X) X(256) X(512) X(1024) X(2048) X(4096)
+#define RS_POW3_PIPE_ROW(X) X(384) X(768) X(1536) X(3072) X(6144)
+#define RS_POW3_PIPE_COL(X) X(384) X(768) X(1536) X(3072) X(6144)
+
+cudaError_t launch_row_pipe_pow2(int n, const RowArgs& a, int* status, cudaStream_t s);
+cudaError_t launch_row_pipe_pow3(int n, const RowArgs& a, int* status, cudaStream_t s);
+cudaError_t launch_col_pipe_pow2(int n, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out,
+                                 int* status, cudaStream_t s);
+cudaError_t launch_col_pipe_pow3(int n, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out,
+                                 int* status, cudaStream_t s);
+// box of the column pipeline for length n: columns per strip and rows per copy; false if none.
+bool col_pipe_box_pow2(int n, int* w, int* bh);
+bool col_pipe_box_pow3(int n, int* w, int* bh);
+bool row_pipe_ok_pow2(int n);
+bool row_pipe_ok_pow3(int n);
 
 #define RS_POW2_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192) X(16384)
 #define RS_POW3_SIZES(X) X(24) X(48) X(96) X(192) X(384) X(768) X(1536) X(3072) X(6144) X(12288)

@@ -1,0 +1,333 @@
+// rs_pipe.cuh — persistent, bulk-copy pipelined versions of the fused row and column passes.
+//
+// Each block owns a sequence of tiles (W whole rows, or a strip of W whole columns) and keeps
+// NB tile buffers in shared memory. While it transforms tile i in buffer i % NB, the bulk-copy
+// engine already fetches tile i+1 into the next buffer (rows: one 1D cp.async.bulk of W*N*8
+// bytes; columns: N/256 2D tensor copies of a W x 256 box). The tile buffer doubles as the FFT
+// exchange buffer (XOR-swizzled addressing) and as the staging area of the result, which one
+// thread writes back with bulk stores. No thread issues a global load or store for the field.
+//
+// Waits on the copy barriers are bounded: after kSpinLimit polls a block records an error in
+// *status and stops; the host reads it with rs_plan_status.
+#pragma once
+#include <cuda.h>
+
+#include "rs_kernels.cuh"
+
+namespace rs {
+
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+// Bounded wait; returns false (and records the failure) when the copy never landed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  if (status) atomicExch(status, 1);
+  return false;
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, const void* src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(smem_addr(src))
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int K>
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(K) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// --------------------------------------------------------------------------- geometry
+template <int N>
+struct RowPipeGeom {
+  static constexpr int T = FftPlan<N>::T;
+  static constexpr int RW = T >= 256 ? 1 : 256 / T;           // rows per tile
+  static constexpr int SLACK = 64;                            // room for a voxel row of nx + 2
+  static constexpr int TILE = RW * (N + SLACK);               // float2 per tile buffer
+  static constexpr int NB = (3 * TILE * 8 <= 200 * 1024) ? 3 : 2;
+  static constexpr int THREADS = RW * T;
+  static constexpr size_t SMEM = static_cast<size_t>(NB) * TILE * sizeof(float2) + NB * sizeof(uint64_t);
+  static constexpr int MINB = (2 * SMEM <= 227 * 1024) ? 2 : 1;  // blocks per SM the registers allow for
+};
+
+template <int N>
+struct ColPipeGeom {
+  static constexpr int T = FftPlan<N>::T;
+  static constexpr int W = T >= 256 ? 2 : 512 / T;            // columns per strip (>= 2: 16-byte boxes)
+  static constexpr int BH = N < 256 ? N : 256;                // rows per tensor-copy box
+  static constexpr int TILE = W * N;
+  static constexpr int NB = (3 * TILE * 8 <= 200 * 1024) ? 3 : 2;
+  static constexpr int THREADS = W * T;
+  static constexpr size_t SMEM = static_cast<size_t>(NB) * TILE * sizeof(float2) + NB * sizeof(uint64_t);
+};
+
+// ---------------------------------------------------------------------- row pipeline
+template <int N>
+__global__ void __launch_bounds__(RowPipeGeom<N>::THREADS, RowPipeGeom<N>::MINB)
+    row_pipe_kernel(const RowArgs a, int* status) {
+  using P = FftPlan<N>;
+  using G = RowPipeGeom<N>;
+  constexpr int T = P::T;
+  constexpr int E = P::E;
+  constexpr int RF = P::entry_radix(false);
+  constexpr int RX = P::exit_radix(false);
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  float2* tiles = reinterpret_cast<float2*>(smem_raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tiles + G::NB * G::TILE);
+  const int t = threadIdx.x % T;
+  const int lr = threadIdx.x / T;
+  const int ntiles = (a.ny + G::RW - 1) / G::RW;
+  const int flags = a.flags;
+  const bool loads = !(flags & ROW_SRC);
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < G::NB; ++b) mbar_init(&bars[b], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  int tile = blockIdx.x;
+  if (threadIdx.x == 0 && loads && tile < ntiles) {
+    const int r0 = tile * G::RW;
+    const uint32_t bytes = static_cast<uint32_t>(min(G::RW, a.ny - r0)) * N * 8u;
+    mbar_arrive_expect(&bars[0], bytes);
+    bulk_load(tiles, a.in + static_cast<size_t>(r0) * N, bytes, &bars[0]);
+  }
+  bool ok = true;
+  for (int i = 0; tile < ntiles && ok; ++i, tile += gridDim.x) {
+    const int b = i % G::NB;
+    float2* tb = tiles + b * G::TILE;
+    const int next = tile + gridDim.x;
+    if (threadIdx.x == 0 && loads && next < ntiles) {
+      bulk_wait_read<G::NB - 2>();  // the buffer's previous store has been read out
+      const int bn = (i + 1) % G::NB;
+      const int r0 = next * G::RW;
+      const uint32_t bytes = static_cast<uint32_t>(min(G::RW, a.ny - r0)) * N * 8u;
+      mbar_arrive_expect(&bars[bn], bytes);
+      bulk_load(tiles + bn * G::TILE, a.in + static_cast<size_t>(r0) * N, bytes, &bars[bn]);
+    }
+    if (loads) {
+      ok = mbar_wait_bounded(&bars[b], (i / G::NB) & 1, status);
+    } else if (threadIdx.x == 0) {
+      bulk_wait_read<G::NB - 1>();  // no loads: the store that last used buffer b has been read out
+    }
+    ok = __syncthreads_and(ok);  // block-uniform: a failed wait stops every thread together
+    if (!ok) break;
+    const int r0 = tile * G::RW;
+    const int rows = min(G::RW, a.ny - r0);
+    const int row = r0 + lr;
+    const bool valid = lr < rows;
+    float2* seq = tb + lr * N;
+    float2 v[E];
+    if (flags & ROW_INV) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = seq[slot_pos<N, RX>(t, e)];
+      __syncthreads();
+      fft_seq<N, true, SwzAddr, 1>(v, seq, t, a.tw);
+    } else if (flags & ROW_SRC) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = point_source_value(a.ps, slot_pos<N, RF>(t, e), row);
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = seq[slot_pos<N, RF>(t, e)];
+      __syncthreads();
+    }
+
+    if (flags & (ROW_TVOX | ROW_TPLASMA)) {
+      const bool vox = flags & ROW_TVOX;
+      const int nxv = vox ? a.vox.nxv : a.pl.nxv;
+      const bool staged = nxv <= N + G::SLACK;
+      float2* vrow = tb + lr * (N + G::SLACK);
+      int yi = -1;
+      float fy = 0.0f;
+      if (valid) {
+        yi = __ldg(&a.ax.yi[row]);
+        if (yi >= 0) fy = __ldg(&a.ax.yf[row]);
+      }
+      if (staged) {
+        if (yi >= 0) {
+          for (int j = t; j < nxv; j += T) vrow[j] = vox ? voxel_col_blend(a.vox, j, yi, fy) : plasma_col_blend(a.pl, j, yi, fy);
+        }
+        __syncthreads();
+      }
+      if (yi >= 0) {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          const int x = slot_pos<N, RF>(t, e);
+          const int xi = __ldg(&a.ax.xi[x]);
+          if (xi >= 0) {
+            const float fx = __ldg(&a.ax.xf[x]);
+            float2 d;
+            if (staged) {
+              d = vrow[xi];
+              if (fx != 0.0f) d = lerp2(d, vrow[xi + 1], fx);
+            } else {
+              d = vox ? voxel_db(a.vox, xi, fx, yi, fy) : plasma_db(a.pl, xi, fx, yi, fy);
+            }
+            if (d.x == 0.0f && d.y == 0.0f) continue;
+            v[e] = cmul(v[e], material_factor(d.x, d.y, vox ? a.vox.a : a.pl.a));
+          }
+        }
+      }
+      if (staged) __syncthreads();
+    }
+
+    if (flags & ROW_FWD) {
+      fft_seq<N, false, SwzAddr, 1>(v, seq, t, a.tw);
+#pragma unroll
+      for (int e = 0; e < E; ++e) seq[slot_pos<N, RX>(t, e)] = (flags & ROW_SCALE) ? cscale(v[e], a.scale) : v[e];
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) seq[slot_pos<N, RF>(t, e)] = (flags & ROW_SCALE) ? cscale(v[e], a.scale) : v[e];
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      bulk_store(a.out + static_cast<size_t>(r0) * N, tb, static_cast<uint32_t>(rows) * N * 8u);
+      bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) bulk_wait_all();
+}
+
+// ------------------------------------------------------------------- column pipeline
+template <int N>
+__global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
+    col_pipe_kernel(const ColArgs a, const __grid_constant__ CUtensorMap map_in,
+                    const __grid_constant__ CUtensorMap map_out, int* status) {
+  using P = FftPlan<N>;
+  using G = ColPipeGeom<N>;
+  constexpr int W = G::W;
+  constexpr int E = P::E;
+  constexpr int RF = P::entry_radix(false);
+  constexpr int RX = P::exit_radix(false);
+  constexpr uint32_t TILE_BYTES = G::TILE * 8u;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  float2* tiles = reinterpret_cast<float2*>(smem_raw);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(tiles + G::NB * G::TILE);
+  const int c = threadIdx.x % W;
+  const int t = threadIdx.x / W;
+  const int nx = a.nx;
+  const int ntiles = (nx + W - 1) / W;
+  const int flags = a.flags;
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < G::NB; ++b) mbar_init(&bars[b], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  int tile = blockIdx.x;
+  if (threadIdx.x == 0 && tile < ntiles) {
+    mbar_arrive_expect(&bars[0], TILE_BYTES);
+    for (int k = 0; k < N / G::BH; ++k) tma_load_2d(tiles + k * G::BH * W, &map_in, tile * W, k * G::BH, &bars[0]);
+  }
+  bool ok = true;
+  for (int i = 0; tile < ntiles && ok; ++i, tile += gridDim.x) {
+    const int b = i % G::NB;
+    float2* tb = tiles + b * G::TILE;
+    const int next = tile + gridDim.x;
+    if (threadIdx.x == 0 && next < ntiles) {
+      bulk_wait_read<G::NB - 2>();
+      const int bn = (i + 1) % G::NB;
+      mbar_arrive_expect(&bars[bn], TILE_BYTES);
+      for (int k = 0; k < N / G::BH; ++k)
+        tma_load_2d(tiles + bn * G::TILE + k * G::BH * W, &map_in, next * W, k * G::BH, &bars[bn]);
+    }
+    ok = __syncthreads_and(mbar_wait_bounded(&bars[b], (i / G::NB) & 1, status));
+    if (!ok) break;
+    const int x = tile * W + c;
+    const bool live = x < nx;
+    float2* col = tb + c;
+    float2 v[E];
+    if (flags & COL_FWD) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = col[slot_pos<N, RF>(t, e) * W];
+      __syncthreads();
+      fft_seq<N, false, SwzAddr, W>(v, col, t, a.tw);
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = col[slot_pos<N, RX>(t, e) * W];
+      __syncthreads();
+    }
+    if (flags & (COL_H | COL_MASK)) {
+      const int lim = live ? __ldg(&a.ylim[x]) : -1;
+      const float2 exv = ((flags & COL_H) && live) ? __ldg(&a.ex[x]) : make_float2(1.f, 0.f);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int fy = slot_pos<N, RX>(t, e);
+        const int m = fy < (N + 1) / 2 ? fy : fy - N;
+        if ((m < 0 ? -m : m) > lim) {
+          v[e] = make_float2(0.f, 0.f);
+        } else if (flags & COL_H) {
+          v[e] = cmul(v[e], cmul(exv, __ldg(&a.ey[fy])));
+        }
+      }
+    }
+    if ((flags & COL_SPEC) && live) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x] = v[e];
+    }
+    if (flags & COL_SCALE) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) v[e] = cscale(v[e], a.scale);
+    }
+    if (flags & COL_INV) {
+      fft_seq<N, true, SwzAddr, W>(v, col, t, a.tw);
+#pragma unroll
+      for (int e = 0; e < E; ++e) col[slot_pos<N, RF>(t, e) * W] = v[e];
+    } else {
+#pragma unroll
+      for (int e = 0; e < E; ++e) col[slot_pos<N, RX>(t, e) * W] = v[e];
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < N / G::BH; ++k) tma_store_2d(&map_out, tile * W, k * G::BH, tb + k * G::BH * W);
+      bulk_commit();
+    }
+  }
+  if (threadIdx.x == 0) bulk_wait_all();
+}
+
+}  // namespace rs

@@ -156,6 +156,13 @@ typedef struct rs_detector_geom {
 int rs_detector(rs_plan* plan, const void* u, double* out, const rs_detector_geom* g,
                 void* stream);
 
+/* Pipelined passes (default on; RS_PIPELINE=0 in the environment turns them off at plan
+ * creation): bulk-copy staged, persistent versions of the fused row / column passes. */
+int rs_plan_set_pipeline(rs_plan* plan, int enable);
+/* Synchronises the device and returns the plan's device status word: 0, or non-zero (with
+ * RS_ETIMEOUT) if a pipelined pass gave up waiting for a bulk copy. */
+int rs_plan_status(rs_plan* plan, int* device_status);
+
 /* Tracing (counterpart of fast-wave's CudaTimerSection, fast-wave/src/simulation.cpp:14-33):
  * total number of kernels this library has launched in the process ... */
 int rs_launch_count(unsigned long long* out);

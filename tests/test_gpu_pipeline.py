@@ -1,0 +1,64 @@
+"""The bulk-copy pipelined passes against the classic passes: same arithmetic in the same order,
+so outputs must be bit-identical; and no bounded wait may have given up."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def run_both(rs, cuda, nx, ny, fn):
+    plan = rs._lib.plan_for(nx, ny, cuda)
+    outs = []
+    for pipe in (False, True):
+        plan.set_pipeline(pipe)
+        outs.append(fn())
+        torch.cuda.synchronize()
+    plan.set_pipeline(True)
+    assert plan.status() == 0
+    return outs
+
+
+@pytest.mark.parametrize("nx,ny", [(4096, 4096), (1024, 2048), (2048, 256), (1536, 1536), (3072, 768), (512, 6144),
+                                   (8192, 512)])
+def test_fft_and_propagate_pipeline_bit_identical(rs, cuda, nx, ny):
+    rng = np.random.default_rng(nx ^ ny)
+    x = (rng.normal(size=nx * ny) + 1j * rng.normal(size=nx * ny)).astype(np.complex64)
+
+    def fn():
+        a = rs.GpuVector.from_numpy(x, cuda)
+        b = rs.GpuVector.zeros(nx * ny, cuda)
+        a.fft2(b, nx, ny)
+        c = rs.GpuVector.zeros(nx * ny, cuda)
+        b.ifft2(c, nx, ny)
+        u, U = rs.GpuVector.from_numpy(x, cuda), rs.GpuVector.zeros(nx * ny, cuda)
+        rs.propagate_2d(u, U, 1e-7, 1.3e-7, 5e-11, 0.01, nx, 3.0e6, nx, ny)
+        rs.propagate_2d(u, U, 1e-7, 1.3e-7, 5e-11, 0.02, nx, 2.5e6, nx, ny, skip_fft=True)
+        return [v.to_numpy() for v in (b, c, u, U)]
+    classic, piped = run_both(rs, cuda, nx, ny, fn)
+    for a, b in zip(classic, piped):
+        np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("n,pitch", [(4096, 1e-6), (2048, 0.5e-6), (1536, 0.37e-6)])
+def test_multislice_pipeline_bit_identical(rs, cuda, n, pitch):
+    wl = rs.convert_energy_wavelength(25000.0)
+    dx = 0.5e-6 if n < 4096 else 0.1e-6
+    gl = int(n * dx / pitch) + 4
+    rng = np.random.default_rng(n)
+    grid = rng.integers(0, 4, size=(6, gl, gl)).astype(np.uint32)
+    s = rs.Sample(z_start=0.5, pixel_size_x=pitch, pixel_size_z=1e-6, grid=grid,
+                  materials=[rs.Material(str(i), 1.0) for i in range(3)], x_positions=np.array([0.1e-6]),
+                  pixel_size_y=pitch, y_positions=np.array([-0.2e-6]))
+    s.db_list = np.array([0, 2e-7 + 1e-10j, 4e-7 + 3e-10j, 1e-7 + 2e-9j])
+    p = rs.SimParams(N=n * n, nx=n, ny=n, dx=dx, dy=dx, z_detector=1.0, detector_size=n * dx,
+                     detector_pixel_size_x=dx, detector_pixel_size_y=dx, wl=wl, chunk_size=n)
+
+    def fn():
+        u, U = rs.GpuVector.zeros(n * n, cuda), rs.GpuVector.zeros(n * n, cuda)
+        rs.propagation.point_source_propagate_2d(u, U, 0.5, 0.0, 0.0, p, 0.45 / dx)
+        s.apply(u, U, p, 0.45 / dx, 0, None)
+        return [u.to_numpy(), U.to_numpy()]
+    classic, piped = run_both(rs, cuda, n, n, fn)
+    for a, b in zip(classic, piped):
+        np.testing.assert_array_equal(a, b)
