@@ -92,11 +92,15 @@ struct RowPipeGeom {
   static constexpr int MINB = (2 * SMEM <= 227 * 1024) ? 2 : 1;  // blocks per SM the registers allow for
 };
 
+// Largest box height <= 256 (the tensor-copy limit) that divides n.
+constexpr int box_rows(int n, int b = 256) { return (b <= 1 || n % b == 0) ? b : box_rows(n, b - 1); }
+
 template <int N>
 struct ColPipeGeom {
   static constexpr int T = FftPlan<N>::T;
   static constexpr int W = T >= 256 ? 2 : 512 / T;            // columns per strip (>= 2: 16-byte boxes)
-  static constexpr int BH = N < 256 ? N : 256;                // rows per tensor-copy box
+  static constexpr int BH = box_rows(N);                      // rows per tensor-copy box
+  static_assert(N % BH == 0, "the boxes must tile a column exactly");
   static constexpr int TILE = W * N;
   static constexpr int NB = (3 * TILE * 8 <= 200 * 1024) ? 3 : 2;
   static constexpr int THREADS = W * T;
