@@ -185,11 +185,12 @@ cudaError_t run_row(rs_plan* p, const RowArgs& r, cudaStream_t s) {
 cudaError_t run_col(rs_plan* p, const ColArgs& c, cudaStream_t s) {
   int w = 0, bh = 0;
   if (p->pipe && col_pipe_box(p->ny, &w, &bh) && aligned16(c.in) && aligned16(c.out) && tensor_map_encoder()) {
+    // Copy the input map before the output lookup: encoding the output may recycle its slot.
     const CUtensorMap* mi = field_map(p, c.in, w, bh);
-    const CUtensorMap* mo = mi ? field_map(p, c.out, w, bh) : nullptr;
-    if (mi && mo) {
-      const CUtensorMap in_copy = *mi;  // field_map may recycle a slot; pass by value
-      return launch_col_pipe(p->ny, c, in_copy, *mo, p->status, s);
+    if (mi) {
+      const CUtensorMap in_copy = *mi;
+      const CUtensorMap* mo = field_map(p, c.out, w, bh);
+      if (mo) return launch_col_pipe(p->ny, c, in_copy, *mo, p->status, s);
     }
   }
   return launch_col_pass(p->ny, c, s);
@@ -825,3 +826,4 @@ int rs_detector(rs_plan* p, const void* u, double* out, const rs_detector_geom* 
 }
 
 }  // extern "C"
+

@@ -57,9 +57,10 @@ def main(root: Path):
         out[f"Al_2.70_{int(e)}"] = delta_beta(db, {"Al": 1}, 2.70, e)
         mu_al = chantler(db, "Al", e, "mu_total")  # cm^2/g
         out[f"Al_mu_total_{int(e)}"] = mu_al
+    out["Al_mu_total_10_50keV_1keV_steps"] = [chantler(db, "Al", 1000.0 * e, "mu_total") for e in range(10, 51)]
     path = Path(__file__).resolve().parent / "chantler_constants.json"
     path.write_text(json.dumps(out, indent=1))
-    print(json.dumps(out, indent=1))
+    print(json.dumps({k: v for k, v in out.items() if not isinstance(v, list)}, indent=1))
 
 
 if __name__ == "__main__":
