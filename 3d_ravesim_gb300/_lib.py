@@ -60,6 +60,7 @@ _SIGS = {
     "rs_detector": ([_P, _P, _P, ctypes.POINTER(DetectorGeom), _P], c_int),
     "rs_plan_set_pipeline": ([_P, c_int], c_int),
     "rs_plan_status": ([_P, ctypes.POINTER(c_int)], c_int),
+    "rs_detector_noalloc": ([_P, c_int, c_int, _P, ctypes.POINTER(DetectorGeom), _P], c_int),
     "rs_launch_count": ([ctypes.POINTER(ctypes.c_ulonglong)], c_int),
     "rs_plan_profile": ([_P, c_int], c_int),
     "rs_plan_profile_read": ([_P, _DP, _DP, ctypes.POINTER(c_int), ctypes.POINTER(c_int)], c_int),

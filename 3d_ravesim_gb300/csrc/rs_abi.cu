@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -827,3 +828,90 @@ int rs_detector(rs_plan* p, const void* u, double* out, const rs_detector_geom* 
 
 }  // extern "C"
 
+// ===================================================================== no-allocation detector
+// rs_detector_noalloc: the detector of rs_detector for callers that must not allocate device
+// memory. Its overlap tables live in this fixed device array instead of a plan-owned buffer.
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 4u << 20;  // 4 MiB: enough for 16384 x 16384 fields
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+void* g_noalloc_addr[kMaxDevices] = {};
+std::once_flag g_noalloc_once[kMaxDevices];
+cudaError_t g_noalloc_setup_err[kMaxDevices] = {};
+
+}  // namespace
+
+extern "C" int rs_detector_noalloc(const void* u, int nx, int ny, double* out, const rs_detector_geom* g,
+                                   void* stream) {
+  if (!u || !out || !g) return fail(RS_EINVAL, "NULL pointer argument");
+  if (nx <= 0 || ny <= 0) return fail(RS_EINVAL, "nx and ny must be positive, got nx=%d, ny=%d", nx, ny);
+  if (g->out_x <= 0 || g->out_y <= 0) return fail(RS_EINVAL, "detector output must be non-empty");
+  if (!finite_pos(g->dx) || !finite_pos(g->dy) || !finite_pos(g->ds_px) || !finite_pos(g->ds_py))
+    return fail(RS_EINVAL, "detector and grid spacings must be positive");
+  if (!std::isfinite(g->detector_z) || g->detector_z == 0.0) return fail(RS_EINVAL, "detector z must be finite and non-zero");
+  int dev = -1;
+  RS_CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(RS_EUNSUPPORTED, "device ordinal %d above %d", dev, kMaxDevices - 1);
+  // Once per device, with that device current: the device address of the scratch array (the
+  // host-side symbol is only a stand-in and must never reach a kernel).
+  std::call_once(g_noalloc_once[dev], [dev] {
+    void* ptr = nullptr;
+    g_noalloc_setup_err[dev] = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    g_noalloc_addr[dev] = ptr;
+  });
+  if (g_noalloc_setup_err[dev] != cudaSuccess || !g_noalloc_addr[dev])
+    return fail(RS_ECUDA, "cudaGetSymbolAddress of the detector scratch failed: %s",
+                cudaGetErrorString(g_noalloc_setup_err[dev]));
+  DetTables t;
+  if (g->integrator == 0) build_area_v1(nx, ny, *g, t);
+  else if (g->integrator == 1) build_legacy(nx, ny, *g, t);
+  else return fail(RS_EINVAL, "unknown integrator %d", g->integrator);
+  const size_t o_xdet = 0;
+  const size_t o_ydet = o_xdet + align8(t.xdet.size() * 8);
+  const size_t o_yw = o_ydet + align8(t.ydet.size() * 8);
+  const size_t o_xw = o_yw + align8(t.yw.size() * 8);
+  const size_t o_xptr = o_xw + align8(t.xw.size() * 4);
+  const size_t o_xcell = o_xptr + align8(t.xptr.size() * 4);
+  const size_t o_yptr = o_xcell + align8(t.xcell.size() * 4);
+  const size_t o_ycell = o_yptr + align8(t.yptr.size() * 4);
+  const size_t total = o_ycell + align8(t.ycell.size() * 4) + 8;
+  if (total > kNoAllocScratchBytes)
+    return fail(RS_EINVAL,
+                "detector tables need %zu bytes but rs_detector_noalloc has a fixed %zu-byte scratch "
+                "(fields up to about 16384 x 16384); use rs_detector for larger fields",
+                total, kNoAllocScratchBytes);
+  std::vector<char> host(total, 0);
+  auto put = [&](size_t off, const void* src, size_t n) { if (n) std::memcpy(host.data() + off, src, n); };
+  put(o_xdet, t.xdet.data(), t.xdet.size() * 8);
+  put(o_ydet, t.ydet.data(), t.ydet.size() * 8);
+  put(o_yw, t.yw.data(), t.yw.size() * 8);
+  put(o_xw, t.xw.data(), t.xw.size() * 4);
+  put(o_xptr, t.xptr.data(), t.xptr.size() * 4);
+  put(o_xcell, t.xcell.data(), t.xcell.size() * 4);
+  put(o_yptr, t.yptr.data(), t.yptr.size() * 4);
+  put(o_ycell, t.ycell.data(), t.ycell.size() * 4);
+  cudaStream_t s = as_stream(stream);
+  char* d = static_cast<char*>(g_noalloc_addr[dev]);
+  // Every entry the kernel reads is rewritten here, so nothing left by an earlier call is used.
+  RS_CK(cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, s));
+  DetArgs a{};
+  a.u = static_cast<const float2*>(u);
+  a.out = out;
+  a.nx = nx;
+  a.out_x = g->out_x;
+  a.out_y = g->out_y;
+  a.xdet = reinterpret_cast<const double*>(d + o_xdet);
+  a.ydet = reinterpret_cast<const double*>(d + o_ydet);
+  a.yw = reinterpret_cast<const double*>(d + o_yw);
+  a.xw = reinterpret_cast<const float*>(d + o_xw);
+  a.xptr = reinterpret_cast<const int*>(d + o_xptr);
+  a.xcell = reinterpret_cast<const int*>(d + o_xcell);
+  a.yptr = reinterpret_cast<const int*>(d + o_yptr);
+  a.ycell = reinterpret_cast<const int*>(d + o_ycell);
+  a.z = g->detector_z;
+  a.accumulate = g->accumulate;
+  RS_CK(launch_detector(a, s));
+  return RS_OK;
+}

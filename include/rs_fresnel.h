@@ -172,6 +172,23 @@ int rs_launch_count(unsigned long long* out);
 int rs_plan_profile(rs_plan* plan, int enable);
 int rs_plan_profile_read(rs_plan* plan, double* row_ms, double* col_ms, int* n_row, int* n_col);
 
+/* The detector of rs_detector for callers that must not allocate device memory: code that
+ * runs where the device memory is owned by someone else (a framework's caching pool, a
+ * fixed memory budget) or that cannot afford rs_detector's cudaMalloc/cudaFree, which grows
+ * its table buffer and synchronises the whole device when it does. This entry point needs no
+ * plan and allocates nothing: its overlap tables (built on the host, copied with one
+ * cudaMemcpyAsync) live in a fixed 4 MiB device array compiled into the library, which is
+ * enough for fields up to about 16384 x 16384; larger requests fail with RS_EINVAL. u is the
+ * (ny, nx) complex64 field, out the float64 (out_y, out_x) image, both device pointers owned
+ * by the caller. The first call on a device looks up that array's device address (with the
+ * caller's device current); make it before any stream capture. All calls share the one
+ * array, so two calls whose work overlaps on the GPU (other streams, other host threads)
+ * race; serialise them. Every table entry is rewritten on each call.
+ * No counterpart in the reference: big-wave allocates its detector output on the host
+ * (propagation.py:700-733). */
+int rs_detector_noalloc(const void* u, int nx, int ny, double* out, const rs_detector_geom* g,
+                        void* stream);
+
 /* Plain (unfused) forms used as the in-repo comparator: T multiply, H multiply. */
 int rs_apply_transmission_voxel(rs_plan* plan, void* u, const void* grid, int grid_signed,
                                 const float* db, int n_db, const rs_voxel_geom* geom,
