@@ -5,6 +5,7 @@ library is missing or fails to load, every call raises RuntimeError.
 """
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import threading
 import weakref
@@ -134,10 +135,12 @@ class Plan:
         self.fast = bool(lib().rs_plan_is_fast(handle))
         self._finalizer = weakref.finalize(self, Plan._destroy, handle, device)
 
-    def set_pipeline(self, enable: bool) -> None:
-        """Select the bulk-copy pipelined passes (default) or the classic per-block passes."""
+    def set_pipeline(self, enable: bool | int) -> None:
+        """Pass variants: True = bulk-copy pipelined rows and columns, False = per-block kernels, or a
+        mask (bit 0 rows, bit 1 columns)."""
+        mask = (3 if enable else 0) if isinstance(enable, bool) else int(enable)
         with torch.cuda.device(self.device):
-            check(lib().rs_plan_set_pipeline(self.handle, 1 if enable else 0), "rs_plan_set_pipeline")
+            check(lib().rs_plan_set_pipeline(self.handle, mask), "rs_plan_set_pipeline")
 
     def status(self) -> int:
         """Synchronise and return the device status word (0 = no bounded wait gave up)."""
@@ -155,13 +158,27 @@ class Plan:
             pass
 
 
-_plans: dict[tuple[int, int, int], Plan] = {}
+_plans: dict[tuple[int, int, int, int], Plan] = {}
+_slot = threading.local()
 
 
-def plan_for(nx: int, ny: int, device: torch.device) -> Plan:
-    """Cached plan per (nx, ny, device). Plans are not shared between threads."""
+@contextlib.contextmanager
+def plan_slot(k: int):
+    """Inside this context, plan_for returns the plans of slot k: work issued on different CUDA
+    streams must use different slots, because a plan's tables are rewritten by each call."""
+    prev = getattr(_slot, "k", 0)
+    _slot.k = int(k)
+    try:
+        yield
+    finally:
+        _slot.k = prev
+
+
+def plan_for(nx: int, ny: int, device: torch.device, slot: int | None = None) -> Plan:
+    """Cached plan per (nx, ny, device, slot). Plans are not shared between threads or streams."""
     idx = device.index if device.index is not None else torch.cuda.current_device()
-    key = (int(nx), int(ny), idx)
+    k = getattr(_slot, "k", 0) if slot is None else int(slot)
+    key = (int(nx), int(ny), idx, k)
     p = _plans.get(key)
     if p is None:
         p = Plan(nx, ny, torch.device("cuda", idx))

@@ -51,6 +51,14 @@ int fail(int code, const char* fmt, ...) {
 
 constexpr int kGenericMax = 6144;
 
+// Default pass variants: the bulk-copy pipeline pays off for the column passes (it replaces 16
+// strided loads per thread); rows keep the per-block kernel, which holds more rows in flight.
+#ifndef RS_DEFAULT_PIPE_ROWS
+#define RS_DEFAULT_PIPE_ROWS 0
+#endif
+constexpr bool kDefaultPipeRows = RS_DEFAULT_PIPE_ROWS != 0;
+constexpr bool kDefaultPipeCols = true;
+
 std::atomic<unsigned long long> g_launches{0};
 
 bool finite_pos(double v) { return std::isfinite(v) && v > 0.0; }
@@ -76,8 +84,9 @@ struct rs_plan {
   float* yf = nullptr;
   void* det = nullptr;
   size_t det_cap = 0;
-  // pipelined (bulk-copy) passes: enabled unless RS_PIPELINE=0 or rs_plan_set_pipeline(plan, 0)
-  bool pipe = true;
+  // pipelined (bulk-copy) passes per direction; RS_PIPELINE / rs_plan_set_pipeline select them
+  bool pipe_rows = true;
+  bool pipe_cols = true;
   int* status = nullptr;  // device word set by bounded waits that gave up
   struct MapEntry {
     const void* ptr = nullptr;
@@ -178,14 +187,14 @@ const CUtensorMap* field_map(rs_plan* p, const void* base, int w, int bh) {
 }
 
 cudaError_t run_row(rs_plan* p, const RowArgs& r, cudaStream_t s) {
-  if (p->pipe && row_pipe_ok(p->nx) && (r.flags & ROW_SRC || aligned16(r.in)) && aligned16(r.out))
+  if (p->pipe_rows && row_pipe_ok(p->nx) && (r.flags & ROW_SRC || aligned16(r.in)) && aligned16(r.out))
     return launch_row_pipe(p->nx, r, p->status, s);
   return launch_row_pass(p->nx, r, s);
 }
 
 cudaError_t run_col(rs_plan* p, const ColArgs& c, cudaStream_t s) {
   int w = 0, bh = 0;
-  if (p->pipe && col_pipe_box(p->ny, &w, &bh) && aligned16(c.in) && aligned16(c.out) && tensor_map_encoder()) {
+  if (p->pipe_cols && col_pipe_box(p->ny, &w, &bh) && aligned16(c.in) && aligned16(c.out) && tensor_map_encoder()) {
     // Copy the input map before the output lookup: encoding the output may recycle its slot.
     const CUtensorMap* mi = field_map(p, c.in, w, bh);
     if (mi) {
@@ -502,8 +511,15 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   p->yi = reinterpret_cast<int*>(c); c += align8(sizeof(int) * ny);
   p->yf = reinterpret_cast<float*>(c); c += align8(sizeof(float) * ny);
   p->status = reinterpret_cast<int*>(c);
+  // RS_PIPELINE: unset -> default; "0" none; "1" both; "rows" / "cols" one direction
   const char* env = std::getenv("RS_PIPELINE");
-  p->pipe = !(env && env[0] == '0');
+  p->pipe_rows = kDefaultPipeRows;
+  p->pipe_cols = kDefaultPipeCols;
+  if (env) {
+    const std::string v(env);
+    p->pipe_rows = v == "1" || v == "rows";
+    p->pipe_cols = v == "1" || v == "cols";
+  }
   e = stage_tw ? launch_stage_twiddles(nx, p->tw_x, 0) : launch_twiddles(p->tw_x, nx, 0);
   if (e == cudaSuccess) e = stage_tw ? launch_stage_twiddles(ny, p->tw_y, 0) : launch_twiddles(p->tw_y, ny, 0);
   if (e == cudaSuccess) e = cudaMemsetAsync(p->status, 0, sizeof(int), 0);
@@ -533,9 +549,10 @@ int rs_plan_destroy(rs_plan* p) {
 
 int rs_plan_is_fast(const rs_plan* p) { return p && p->fast ? 1 : 0; }
 
-int rs_plan_set_pipeline(rs_plan* p, int enable) {
+int rs_plan_set_pipeline(rs_plan* p, int mask) {
   RS_TRY(check_plan(p));
-  p->pipe = enable != 0;
+  p->pipe_rows = (mask & 1) != 0;
+  p->pipe_cols = (mask & 2) != 0;
   return RS_OK;
 }
 

@@ -215,8 +215,17 @@ __device__ __forceinline__ float2 point_source_value(const PointSrcArgs& p, int 
 }
 
 // ----------------------------------------------------------------------------- row pass
+#ifndef RS_ROW_MINB
+#define RS_ROW_MINB 3
+#endif
+// blocks per SM the row pass's registers are sized for (one 256-thread row block: 3 -> <= 85 regs)
 template <int N, int ROWS>
-__global__ void __launch_bounds__(ROWS * FftPlan<N>::T) row_pass_kernel(const RowArgs a) {
+constexpr int row_minb() {
+  return ROWS * FftPlan<N>::T <= 256 ? (FftPlan<N>::E == 16 ? RS_ROW_MINB : 2) : 1;
+}
+
+template <int N, int ROWS>
+__global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row_pass_kernel(const RowArgs a) {
   using P = FftPlan<N>;
   constexpr int T = P::T;
   constexpr int RF = P::entry_radix(false);   // forward entry == inverse exit mapping
@@ -264,23 +273,34 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T) row_pass_kernel(const Ro
       }
       __syncthreads();
     }
-    if (yi >= 0) {
+    // Branch-free over the E pixels of this thread so their gathers and transcendentals
+    // interleave; vacuum (delta = beta = 0) gives a factor of exactly 1. A warp whose pixels are
+    // all vacuum skips the transcendentals.
+    constexpr int CH = E % 8 == 0 ? 8 : E;  // pixels per interleaved chunk
 #pragma unroll
-      for (int e = 0; e < E; ++e) {
-        const int x = slot_pos<N, RF>(t, e);
-        const int xi = __ldg(&a.ax.xi[x]);
+    for (int c0 = 0; c0 < E; c0 += CH) {
+      float2 d[CH];
+      bool any = false;
+#pragma unroll
+      for (int i = 0; i < CH; ++i) {
+        d[i] = make_float2(0.f, 0.f);
+        const int x = slot_pos<N, RF>(t, c0 + i);
+        const int xi = yi >= 0 ? __ldg(&a.ax.xi[x]) : -1;
         if (xi >= 0) {
           const float fx = __ldg(&a.ax.xf[x]);
-          float2 d;
           if (staged) {
-            d = buf[xi];
-            if (fx != 0.0f) d = lerp2(d, buf[xi + 1], fx);
+            d[i] = buf[xi];
+            if (fx != 0.0f) d[i] = lerp2(d[i], buf[xi + 1], fx);
           } else {
-            d = vox ? voxel_db(a.vox, xi, fx, yi, fy) : plasma_db(a.pl, xi, fx, yi, fy);
+            d[i] = vox ? voxel_db(a.vox, xi, fx, yi, fy) : plasma_db(a.pl, xi, fx, yi, fy);
           }
-          if (d.x == 0.0f && d.y == 0.0f) continue;  // vacuum: factor exactly 1
-          v[e] = cmul(v[e], material_factor(d.x, d.y, vox ? a.vox.a : a.pl.a));
+          any |= (d[i].x != 0.0f) | (d[i].y != 0.0f);
         }
+      }
+      if (__any_sync(0xffffffffu, any)) {
+        const float at = vox ? a.vox.a : a.pl.a;
+#pragma unroll
+        for (int i = 0; i < CH; ++i) v[c0 + i] = cmul(v[c0 + i], material_factor(d[i].x, d[i].y, at));
       }
     }
     if (staged) __syncthreads();  // the forward transform reuses the buffer

@@ -86,10 +86,15 @@ struct RowPipeGeom {
   static constexpr int RW = T >= 256 ? 1 : 256 / T;           // rows per tile
   static constexpr int SLACK = 64;                            // room for a voxel row of nx + 2
   static constexpr int TILE = RW * (N + SLACK);               // float2 per tile buffer
+#ifdef RS_ROWPIPE_NB
+  static constexpr int NB = RS_ROWPIPE_NB;
+#else
   static constexpr int NB = (3 * TILE * 8 <= 200 * 1024) ? 3 : 2;
+#endif
   static constexpr int THREADS = RW * T;
   static constexpr size_t SMEM = static_cast<size_t>(NB) * TILE * sizeof(float2) + NB * sizeof(uint64_t);
-  static constexpr int MINB = (2 * SMEM <= 227 * 1024) ? 2 : 1;  // blocks per SM the registers allow for
+  // blocks per SM the register budget is sized for (as many as shared memory admits, up to 3)
+  static constexpr int MINB = (3 * SMEM <= 227 * 1024) ? 3 : (2 * SMEM <= 227 * 1024) ? 2 : 1;
 };
 
 // Largest box height <= 256 (the tensor-copy limit) that divides n.
@@ -195,23 +200,33 @@ __global__ void __launch_bounds__(RowPipeGeom<N>::THREADS, RowPipeGeom<N>::MINB)
         }
         __syncthreads();
       }
-      if (yi >= 0) {
+      // Branch-free over the E pixels (their gathers and transcendentals interleave); vacuum
+      // gives a factor of exactly 1; an all-vacuum warp skips the transcendentals.
+      constexpr int CH = E % 8 == 0 ? 8 : E;  // pixels per interleaved chunk
 #pragma unroll
-        for (int e = 0; e < E; ++e) {
-          const int x = slot_pos<N, RF>(t, e);
-          const int xi = __ldg(&a.ax.xi[x]);
+      for (int c0 = 0; c0 < E; c0 += CH) {
+        float2 d[CH];
+        bool any = false;
+#pragma unroll
+        for (int i = 0; i < CH; ++i) {
+          d[i] = make_float2(0.f, 0.f);
+          const int x = slot_pos<N, RF>(t, c0 + i);
+          const int xi = yi >= 0 ? __ldg(&a.ax.xi[x]) : -1;
           if (xi >= 0) {
             const float fx = __ldg(&a.ax.xf[x]);
-            float2 d;
             if (staged) {
-              d = vrow[xi];
-              if (fx != 0.0f) d = lerp2(d, vrow[xi + 1], fx);
+              d[i] = vrow[xi];
+              if (fx != 0.0f) d[i] = lerp2(d[i], vrow[xi + 1], fx);
             } else {
-              d = vox ? voxel_db(a.vox, xi, fx, yi, fy) : plasma_db(a.pl, xi, fx, yi, fy);
+              d[i] = vox ? voxel_db(a.vox, xi, fx, yi, fy) : plasma_db(a.pl, xi, fx, yi, fy);
             }
-            if (d.x == 0.0f && d.y == 0.0f) continue;
-            v[e] = cmul(v[e], material_factor(d.x, d.y, vox ? a.vox.a : a.pl.a));
+            any |= (d[i].x != 0.0f) | (d[i].y != 0.0f);
           }
+        }
+        if (__any_sync(0xffffffffu, any)) {
+          const float at = vox ? a.vox.a : a.pl.a;
+#pragma unroll
+          for (int i = 0; i < CH; ++i) v[c0 + i] = cmul(v[c0 + i], material_factor(d[i].x, d[i].y, at));
         }
       }
       if (staged) __syncthreads();

@@ -140,3 +140,33 @@ def talbot_lau(n: int = 4096, slices: int = 512, seed: int = 0, dx: float = 0.1e
                     info={"nx": n, "ny": n, "energy_ev": energy, "sample_slices": slices, "blobs": blobs,
                           "voxel_grid": [slices, length, length], "talbot_distance_m": d_t,
                           "g1_thickness_m": t1, "g2_beta": beta_g2})
+
+
+def gaussian_plasma(n: int = 2048, slices: int = 256, dx: float = 0.5e-6, energy: float = 8000.0,
+                    n0: float = 1e21, length: float = 150e-6, te: float = 500.0, zstar: float = 3.5,
+                    pz: float = 2e-6, pitch: float = 2e-6, z_detector_gap: float = 0.2):
+    """Config-3 forward: a plasma with n_e = n0 exp(-r^2 / 2 L^2) (cm^-3, r from the centre of the
+    slab), T_e = 500 eV, Z* = 3.5 and n_i = n_e / Z*, in CH (zbar = 3.5, z2bar = 18.5), so q = 1 and
+    only the free-electron refraction and the Kramers absorption contribute."""
+    from .plasma_sample import PlasmaSample
+    wl = convert_energy_wavelength(energy)
+    fov = n * dx
+    glen = int(math.ceil(fov / pitch)) + 4
+    glen += glen % 2
+    ax = (np.arange(glen) - glen / 2.0) * pitch
+    zc = (np.arange(slices) + 0.5 - slices / 2.0) * pz
+    r2xy = ax[None, :] ** 2 + ax[:, None] ** 2
+    ne = np.empty((slices, glen, glen), dtype=np.float32)
+    for k in range(slices):
+        ne[k] = n0 * np.exp(-(r2xy + zc[k] ** 2) / (2.0 * length ** 2))
+    ni = (ne / zstar).astype(np.float32)
+    teg = np.full_like(ne, te)
+    zs = np.full_like(ne, zstar)
+    z0 = 0.1
+    sample = PlasmaSample(z_start=z0, pixel_size_x=pitch, pixel_size_z=pz, ne_grid=ne, ni_grid=ni, te_grid=teg,
+                          zstar_grid=zs, Z=6, x_positions=np.array([0.0]), formula="CH", pixel_size_y=pitch,
+                          y_positions=np.array([0.0]), scattering_factors=(6.0, 0.0, 3.5, 18.5))
+    p = SimParams(N=n * n, nx=n, ny=n, dx=dx, dy=dx, z_detector=z0 + slices * pz + z_detector_gap,
+                  detector_size=fov, detector_pixel_size_x=dx, detector_pixel_size_y=dx, wl=wl, chunk_size=n)
+    return Workload("gaussian_plasma", p, [sample], cutoff=0.45 / dx, source_xyz=None, z_first=z0,
+                    info={"nx": n, "ny": n, "slices": slices, "energy_ev": energy, "grid": [slices, glen, glen]})

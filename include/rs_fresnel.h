@@ -156,9 +156,10 @@ typedef struct rs_detector_geom {
 int rs_detector(rs_plan* plan, const void* u, double* out, const rs_detector_geom* g,
                 void* stream);
 
-/* Pipelined passes (default on; RS_PIPELINE=0 in the environment turns them off at plan
- * creation): bulk-copy staged, persistent versions of the fused row / column passes. */
-int rs_plan_set_pipeline(rs_plan* plan, int enable);
+/* Pass variants: bulk-copy staged, persistent versions of the fused passes. mask bit 0 selects
+ * them for the row passes, bit 1 for the column passes (default: columns only). RS_PIPELINE in
+ * the environment ("0", "1", "rows", "cols") overrides the default at plan creation. */
+int rs_plan_set_pipeline(rs_plan* plan, int mask);
 /* Synchronises the device and returns the plan's device status word: 0, or non-zero (with
  * RS_ETIMEOUT) if a pipelined pass gave up waiting for a bulk copy. */
 int rs_plan_status(rs_plan* plan, int* device_status);

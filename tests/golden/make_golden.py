@@ -38,13 +38,14 @@ def import_reference(root: Path):
     sys.modules.update({"bfpy": bf, "ruamel": ru, "ruamel.yaml": ry, "ruamel.yaml.comments": ryc,
                         "h5py": types.ModuleType("h5py"), "nist_lookup.xraydb_plugin": xp})
     import config  # noqa: F401  (must precede the others)
+    import multisim
     import optical_element
     import plasma_sample
     import propagation
     import source
     import vector
     import wavesim
-    return propagation, optical_element, plasma_sample, source, vector, wavesim
+    return propagation, optical_element, plasma_sample, source, vector, wavesim, multisim
 
 
 def cfield(rng, ny, nx, dtype):
@@ -52,7 +53,7 @@ def cfield(rng, ny, nx, dtype):
 
 
 def main(root: Path) -> None:
-    prop, oe, ps, src, vec, ws = import_reference(root)
+    prop, oe, ps, src, vec, ws, ms = import_reference(root)
     NV = vec.NumpyVector
     rng = np.random.default_rng(20261203)
     g: dict[str, np.ndarray] = {}
@@ -192,6 +193,12 @@ def main(root: Path) -> None:
     g["run_u"] = u.vec.reshape(ny, nx)
     g["run_grid"] = grid2
     g["run_params"] = np.array([*angles, wl20])
+
+    # -- generate_energies_from_spectrum (multisim.py:695-724) ---------------------------
+    e = np.arange(10, 51, dtype=np.float64) * 1e3
+    inten = np.clip((45e3 - e) / e, 0, None) * np.exp(-np.linspace(6.9, 0.1, e.size))
+    g["spectrum_e"], g["spectrum_i"] = e, inten
+    g["spectrum_draw"] = ms.generate_energies_from_spectrum(e, inten, np.random.RandomState(11), (15e3, 40e3), 64)
 
     # big-wave mutates U.vec in place (modify_chunked), so every stored array is a copy
     np.savez_compressed(OUT, **{k: np.array(v, copy=True) for k, v in g.items()})

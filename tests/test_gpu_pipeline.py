@@ -10,11 +10,11 @@ pytestmark = pytest.mark.gpu
 def run_both(rs, cuda, nx, ny, fn):
     plan = rs._lib.plan_for(nx, ny, cuda)
     outs = []
-    for pipe in (False, True):
-        plan.set_pipeline(pipe)
+    for mask in (0, 1, 2, 3):  # per-block kernels, pipelined rows, pipelined columns, both
+        plan.set_pipeline(mask)
         outs.append(fn())
         torch.cuda.synchronize()
-    plan.set_pipeline(True)
+    plan.set_pipeline(2)
     assert plan.status() == 0
     return outs
 
@@ -35,9 +35,10 @@ def test_fft_and_propagate_pipeline_bit_identical(rs, cuda, nx, ny):
         rs.propagate_2d(u, U, 1e-7, 1.3e-7, 5e-11, 0.01, nx, 3.0e6, nx, ny)
         rs.propagate_2d(u, U, 1e-7, 1.3e-7, 5e-11, 0.02, nx, 2.5e6, nx, ny, skip_fft=True)
         return [v.to_numpy() for v in (b, c, u, U)]
-    classic, piped = run_both(rs, cuda, nx, ny, fn)
-    for a, b in zip(classic, piped):
-        np.testing.assert_array_equal(a, b)
+    runs = run_both(rs, cuda, nx, ny, fn)
+    for other in runs[1:]:
+        for a, b in zip(runs[0], other):
+            np.testing.assert_array_equal(a, b)
 
 
 @pytest.mark.parametrize("n,pitch", [(4096, 1e-6), (2048, 0.5e-6), (1536, 0.37e-6)])
@@ -59,6 +60,7 @@ def test_multislice_pipeline_bit_identical(rs, cuda, n, pitch):
         rs.propagation.point_source_propagate_2d(u, U, 0.5, 0.0, 0.0, p, 0.45 / dx)
         s.apply(u, U, p, 0.45 / dx, 0, None)
         return [u.to_numpy(), U.to_numpy()]
-    classic, piped = run_both(rs, cuda, n, n, fn)
-    for a, b in zip(classic, piped):
-        np.testing.assert_array_equal(a, b)
+    runs = run_both(rs, cuda, n, n, fn)
+    for other in runs[1:]:
+        for a, b in zip(runs[0], other):
+            np.testing.assert_array_equal(a, b)
