@@ -53,6 +53,9 @@ _SIGS = {
     "rs_point_source": ([_P, _P, c_double, c_double, c_double, c_double, c_double, c_double, _P], c_int),
     "rs_point_source_propagate": ([_P, _P, _P, c_double, c_double, c_double, c_double, c_double,
                                    c_double, c_double, _P], c_int),
+    "rs_fresnel_plane": ([_P, _P, c_double, c_double, c_double, c_double, c_double, c_double, _P], c_int),
+    "rs_fresnel_plane_propagate": ([_P, _P, _P, c_double, c_double, c_double, c_double, c_double, c_double,
+                                    c_double, _P], c_int),
     "rs_multislice_voxel": ([_P, _P, _P, _P, c_int, _P, c_int, ctypes.POINTER(VoxelGeom), c_double,
                              c_double, c_double, c_double, _DP, _DP, c_int, c_int, _P], c_int),
     "rs_multislice_plasma": ([_P, _P, _P, _P, _P, _P, _P, c_int, ctypes.POINTER(PlasmaConsts),

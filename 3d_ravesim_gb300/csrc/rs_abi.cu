@@ -680,15 +680,48 @@ int rs_point_source(rs_plan* p, void* u, double dx, double dy, double xs, double
   return RS_OK;
 }
 
+static int source_propagate(rs_plan* p, void* u_, void* U_, const PointSrcArgs& a, double dx, double dy,
+                            double wl, double cutoff, void* stream);
+
 int rs_point_source_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double xs,
                               double ys, double z, double wl, double cutoff, void* stream) {
   RS_TRY(check_plan(p));
   if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
+  PointSrcArgs a{};
+  RS_TRY(point_args(p, dx, dy, xs, ys, z, wl, a));
+  return source_propagate(p, u_, U_, a, dx, dy, wl, cutoff, stream);
+}
+
+int rs_fresnel_plane(rs_plan* p, void* u, double dx, double dy, double xs, double ys, double dz, double wl,
+                     void* stream) {
+  RS_TRY(check_plan(p));
+  if (!u) return fail(RS_EINVAL, "NULL field pointer");
+  if (!(dz > 0.0) || !std::isfinite(dz)) return fail(RS_EINVAL, "Fresnel source-to-sample distance must be positive");
+  PointSrcArgs a{};
+  RS_TRY(point_args(p, dx, dy, xs, ys, 0.0, wl, a));
+  a.fresnel_plane = 1;
+  a.dz = dz;
+  RS_CK(launch_point_source(static_cast<float2*>(u), p->nx, p->ny, a, as_stream(stream)));
+  return RS_OK;
+}
+
+int rs_fresnel_plane_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double xs, double ys,
+                               double dz, double wl, double cutoff, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
+  if (!(dz > 0.0) || !std::isfinite(dz)) return fail(RS_EINVAL, "Fresnel source-to-sample distance must be positive");
+  PointSrcArgs a{};
+  RS_TRY(point_args(p, dx, dy, xs, ys, 0.0, wl, a));
+  a.fresnel_plane = 1;
+  a.dz = dz;
+  return source_propagate(p, u_, U_, a, dx, dy, wl, cutoff, stream);
+}
+
+static int source_propagate(rs_plan* p, void* u_, void* U_, const PointSrcArgs& a, double dx, double dy,
+                            double wl, double cutoff, void* stream) {
   float2* u = static_cast<float2*>(u_);
   float2* U = static_cast<float2*>(U_);
   cudaStream_t s = as_stream(stream);
-  PointSrcArgs a{};
-  RS_TRY(point_args(p, dx, dy, xs, ys, z, wl, a));
   RS_TRY(build_prop(p, dx, dy, wl, 0.0, cutoff, false, s));
   if (p->fast) {
     RowArgs r{};

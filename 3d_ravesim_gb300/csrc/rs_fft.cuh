@@ -62,6 +62,13 @@ struct FftPlan {
   }
   __host__ __device__ static constexpr int table_len(bool inv) { return stage_offset(inv, NST); }
   static constexpr int N_TW = table_len(false);
+  // palindromic radix list: the inverse stages see the same (Ns, R) as the forward ones, so they
+  // read the forward table (conjugated on use) and the inverse copy is never touched
+  __host__ __device__ static constexpr bool symmetric(int s = 0) {
+    return s >= NST ? true : (radix(false, s) == radix(true, s) && symmetric(s + 1));
+  }
+  static constexpr int INV_BASE = symmetric() ? 0 : N_TW;
+  static constexpr int TW_USED = symmetric() ? N_TW : N_TW + table_len(true);
 };
 
 __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
@@ -88,7 +95,16 @@ __device__ __forceinline__ void dft_all(float2 (&v)[E], std::integer_sequence<in
   (dft_slice<R, INV, Bs * R, E>(v), ...);
 }
 
-template <int N, bool INV, int SI, int NS, class AD = PadAddr, int STR = 1>
+// Twiddle-load policies: from global memory through the read-only path, or from a copy of the
+// table in shared memory (a generic pointer into the block's shared window).
+struct TwGlobal {
+  static __device__ __forceinline__ float2 load(const float2* p) { return __ldg(p); }
+};
+struct TwShared {
+  static __device__ __forceinline__ float2 load(const float2* p) { return *p; }
+};
+
+template <int N, bool INV, int SI, int NS, class AD = PadAddr, int STR = 1, class TWL = TwGlobal>
 struct FftStages {
   using P = FftPlan<N>;
   static __device__ __forceinline__ void run(float2 (&v)[P::E], float2* buf, int t,
@@ -102,7 +118,7 @@ struct FftStages {
       for (int b = 0; b < B; ++b) {
         const int k = (t + b * T) % NS;
 #if RS_TW_STAGE_MAJOR
-        constexpr int TW_OFF = (INV ? P::N_TW : 0) + P::stage_offset(INV, SI);
+        constexpr int TW_OFF = (INV ? P::INV_BASE : 0) + P::stage_offset(INV, SI);
         const float2* tws = tw + TW_OFF + k;
 #else
         const int step = k * (N / (NS * R));
@@ -110,9 +126,9 @@ struct FftStages {
 #pragma unroll
         for (int r = 1; r < R; ++r) {
 #if RS_TW_STAGE_MAJOR
-          const float2 w = __ldg(&tws[(r - 1) * NS]);
+          const float2 w = TWL::load(&tws[(r - 1) * NS]);
 #else
-          const float2 w = __ldg(&tw[r * step]);
+          const float2 w = TWL::load(&tw[r * step]);
 #endif
           v[b * R + r] = INV ? cmulc(v[b * R + r], w) : cmul(v[b * R + r], w);
         }
@@ -132,7 +148,7 @@ struct FftStages {
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = buf[AD::at(slot_pos<N, R2>(t, e)) * STR];
       __syncthreads();
-      FftStages<N, INV, SI + 1, NS * R, AD, STR>::run(v, buf, t, tw);
+      FftStages<N, INV, SI + 1, NS * R, AD, STR, TWL>::run(v, buf, t, tw);
     }
   }
 };
@@ -140,10 +156,10 @@ struct FftStages {
 // Full transform of one sequence. On entry v is in the entry mapping of this direction,
 // on exit in its exit mapping. Every thread of the block must call it (it synchronises).
 // tw: the stage-major tables (RS_TW_STAGE_MAJOR) or tw[m] = exp(-2*pi*i*m/N), m in [0, N).
-template <int N, bool INV, class AD = PadAddr, int STR = 1>
+template <int N, bool INV, class AD = PadAddr, int STR = 1, class TWL = TwGlobal>
 __device__ __forceinline__ void fft_seq(float2 (&v)[FftPlan<N>::E], float2* buf, int t,
                                         const float2* __restrict__ tw) {
-  FftStages<N, INV, 0, 1, AD, STR>::run(v, buf, t, tw);
+  FftStages<N, INV, 0, 1, AD, STR, TWL>::run(v, buf, t, tw);
 }
 
 }  // namespace rs

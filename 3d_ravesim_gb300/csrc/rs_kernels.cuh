@@ -61,6 +61,8 @@ struct PlasmaArgs {
 struct PointSrcArgs {
   double dx, dy, xs, ys, z2, k;  // k = (2*pi)/wl exactly as numpy forms it
   double half_nx, half_ny;
+  int fresnel_plane;             // 1: Fresnel-scaled plane exp(-i k (x xs + y ys)/dz)/dz
+  double dz;                     // source-to-plane distance of the Fresnel-scaled plane
 };
 
 struct RowArgs {
@@ -199,7 +201,24 @@ constexpr double kInv2PiLo = -9.839338337591243e-18;
 // big-wave/propagation.py:474-483: the FP64 phase phi = r*k is formed with the same IEEE
 // operations as numpy, then reduced to a fraction of a cycle with a double-double 1/(2*pi)
 // (error ~|phi|*2^-106) before a single-precision sincospi.
+// Fresnel-scaled source plane (big-wave/source.py:81-90): x = (ix - nx/2) dx,
+// phase = -k (x xs + y ys) / dz formed in FP64 like numpy, value exp(i phase) / dz.
+__device__ __forceinline__ float2 fresnel_plane_value(const PointSrcArgs& p, int ix, int iy) {
+  const double x = __dmul_rn(__dsub_rn(static_cast<double>(ix), p.half_nx), p.dx);
+  const double y = __dmul_rn(__dsub_rn(static_cast<double>(iy), p.half_ny), p.dy);
+  const double phi = -__ddiv_rn(__dmul_rn(p.k, __dadd_rn(__dmul_rn(x, p.xs), __dmul_rn(y, p.ys))), p.dz);
+  const double c_hi = __dmul_rn(phi, kInv2PiHi);
+  const double c_err = __fma_rn(phi, kInv2PiHi, -c_hi);
+  const double n = rint(c_hi);
+  const double f = __dadd_rn(__dsub_rn(c_hi, n), __fma_rn(phi, kInv2PiLo, c_err));
+  float s, c;
+  sincospif(static_cast<float>(2.0 * f), &s, &c);
+  const float inv = static_cast<float>(1.0 / p.dz);
+  return make_float2(c * inv, s * inv);
+}
+
 __device__ __forceinline__ float2 point_source_value(const PointSrcArgs& p, int ix, int iy) {
+  if (p.fresnel_plane) return fresnel_plane_value(p, ix, iy);
   const double x = __dsub_rn(__dmul_rn(__dsub_rn(static_cast<double>(ix), p.half_nx), p.dx), p.xs);
   const double y = __dsub_rn(__dmul_rn(__dsub_rn(static_cast<double>(iy), p.half_ny), p.dy), p.ys);
   const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(y, y), __dmul_rn(x, x)), p.z2));

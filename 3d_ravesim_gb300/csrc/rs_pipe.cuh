@@ -12,6 +12,8 @@
 #pragma once
 #include <cuda.h>
 
+#include <type_traits>
+
 #include "rs_kernels.cuh"
 
 namespace rs {
@@ -109,7 +111,16 @@ struct ColPipeGeom {
   static constexpr int TILE = W * N;
   static constexpr int NB = (3 * TILE * 8 <= 200 * 1024) ? 3 : 2;
   static constexpr int THREADS = W * T;
-  static constexpr size_t SMEM = static_cast<size_t>(NB) * TILE * sizeof(float2) + NB * sizeof(uint64_t);
+  // twiddles (forward and inverse stage-major tables) copied to shared memory when they fit
+  static constexpr int TW_LEN = FftPlan<N>::TW_USED;
+  static constexpr size_t TILES_BYTES = static_cast<size_t>(NB) * TILE * sizeof(float2);
+  static constexpr size_t TW_BYTES = static_cast<size_t>((TW_LEN + 1) / 2 * 2) * sizeof(float2);
+#ifndef RS_COLPIPE_TW_SMEM
+#define RS_COLPIPE_TW_SMEM 1
+#endif
+  static constexpr bool TW_SMEM =
+      RS_COLPIPE_TW_SMEM && RS_TW_STAGE_MAJOR && TW_LEN > 0 && TILES_BYTES + TW_BYTES + 64 <= 227 * 1024;
+  static constexpr size_t SMEM = TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + NB * sizeof(uint64_t);
 };
 
 // ---------------------------------------------------------------------- row pipeline
@@ -264,7 +275,8 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
   constexpr uint32_t TILE_BYTES = G::TILE * 8u;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   float2* tiles = reinterpret_cast<float2*>(smem_raw);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(tiles + G::NB * G::TILE);
+  float2* tw_s = tiles + G::NB * G::TILE;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + G::TILES_BYTES + (G::TW_SMEM ? G::TW_BYTES : 0));
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
   const int nx = a.nx;
@@ -276,6 +288,12 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
   }
   __syncthreads();
 
+  if constexpr (G::TW_SMEM) {  // the block's copy of the twiddle tables (read from L2 once)
+    for (int i = threadIdx.x; i < G::TW_LEN; i += blockDim.x) tw_s[i] = __ldg(&a.tw[i]);
+    __syncthreads();
+  }
+  const float2* tw = G::TW_SMEM ? tw_s : a.tw;
+  using TWL = typename std::conditional<G::TW_SMEM, TwShared, TwGlobal>::type;
   int tile = blockIdx.x;
   if (threadIdx.x == 0 && tile < ntiles) {
     mbar_arrive_expect(&bars[0], TILE_BYTES);
@@ -303,7 +321,7 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = col[slot_pos<N, RF>(t, e) * W];
       __syncthreads();
-      fft_seq<N, false, SwzAddr, W>(v, col, t, a.tw);
+      fft_seq<N, false, SwzAddr, W, TWL>(v, col, t, tw);
     } else {
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = col[slot_pos<N, RX>(t, e) * W];
@@ -332,7 +350,7 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
       for (int e = 0; e < E; ++e) v[e] = cscale(v[e], a.scale);
     }
     if (flags & COL_INV) {
-      fft_seq<N, true, SwzAddr, W>(v, col, t, a.tw);
+      fft_seq<N, true, SwzAddr, W, TWL>(v, col, t, tw);
 #pragma unroll
       for (int e = 0; e < E; ++e) col[slot_pos<N, RF>(t, e) * W] = v[e];
     } else {

@@ -3,7 +3,7 @@ from __future__ import annotations
 
 from dataclasses import dataclass
 
-from .propagation import SimParams, grid_density_check_2d, point_source_propagate_2d
+from .propagation import SimParams, fresnel_plane_propagate_2d, grid_density_check_2d, point_source_propagate_2d
 
 
 @dataclass
@@ -20,7 +20,16 @@ class PointSource:
         if not sim_params.is_2d:
             raise NotImplementedError("the GB300 PointSource implements the 2D path (ny > 1)")
         if sim_params.use_fresnel_scaling:
-            raise NotImplementedError("Fresnel-scaled plane initialisation is not part of this build")
+            # big-wave/source.py:62-95: the incident spherical phase is removed; the plane carries the
+            # off-axis linear phase ramp and the 1/dz amplitude
+            if sim_params.fresnel_effective_z <= 0 or sim_params.fresnel_magnification <= 0:
+                raise ValueError("Fresnel detector geometry has not been configured")
+            if dz <= 0:
+                raise ValueError("Fresnel source-to-sample distance must be positive")
+            if history is not None:
+                raise ValueError("physical-z source history is not supported with Fresnel scaling")
+            fresnel_plane_propagate_2d(u, U, dz, self.x, self.y, sim_params, cutoff_freq)
+            return
         if history is not None:
             raise NotImplementedError("analytic source history is not part of this build")
         grid_density_check_2d(dz, self.x, sim_params.nx, sim_params.dx, self.y, sim_params.ny,

@@ -91,6 +91,15 @@ int rs_point_source_propagate(rs_plan* plan, void* u, void* U, double dx, double
                               double xs, double ys, double z, double wl, double cutoff,
                               void* stream);
 
+/* Fresnel-scaled source plane u = exp(-2 pi i (x xs + y ys)/(wl dz)) / dz, x = (ix - nx/2) dx (FP64
+ * phase reduced to cycles), and the same followed by FFT2, circular cutoff and IFFT2 (U left
+ * holding the cut-off spectrum). Replace the Fresnel-scaling branch of PointSource.propagate_to
+ * (big-wave/source.py:62-95), after its geometry checks. */
+int rs_fresnel_plane(rs_plan* plan, void* u, double dx, double dy, double xs, double ys, double dz,
+                     double wl, void* stream);
+int rs_fresnel_plane_propagate(rs_plan* plan, void* u, void* U, double dx, double dy, double xs,
+                               double ys, double dz, double wl, double cutoff, void* stream);
+
 /* Geometry of a voxel Sample (big-wave/optical_element.py:383-412, 502-546). */
 typedef struct rs_voxel_geom {
   int nz, ny_v, nx_v;        /* grid shape (z, y, x)                                   */

@@ -95,6 +95,18 @@ def point_source_2d(nx, ny, dx, dy, z, xs, ys, wl, cutoff, dtype=np.complex128):
     return ifft2(U), U
 
 
+def fresnel_plane_2d(nx, ny, dx, dy, dz, xs, ys, wl, cutoff, dtype=np.complex128):
+    """Fresnel-scaled source plane, FFT2, cutoff, IFFT2 (big-wave/source.py:62-95)."""
+    wave_number = 2.0 * np.pi / wl
+    flat = np.arange(nx * ny, dtype=np.int64)
+    x = (flat % nx - nx / 2.0) * dx
+    y = (flat // nx - ny / 2.0) * dy
+    phase = -wave_number * (x * xs + y * ys) / dz
+    u = (np.exp(1j * phase) / dz).astype(dtype).reshape(ny, nx)
+    U = apply_frequency_cutoff_2d(fft2(u), cutoff, dx, dy)
+    return ifft2(U), U
+
+
 def material_factor(deltabeta, thickness: float, wl: float):
     """big-wave/optical_element.py:39-42."""
     return np.exp(-2j * np.pi * thickness / wl * np.conj(deltabeta))

@@ -103,6 +103,17 @@ def main(root: Path) -> None:
         g[f"ps_prop_{name}_u"], g[f"ps_prop_{name}_U"] = u.vec.reshape(64, 64).copy(), U.vec.reshape(64, 64).copy()
     g["ps_prop_params"] = np.array([64, 64, 1e-6, 1e-6, 2.0, 3e-6, -2e-6, p2.wl, 0.3e6])
 
+    # -- Fresnel-scaled source plane (source.py:62-95) -----------------------------------
+    pf = prop.SimParams(N=64 * 48, nx=64, ny=48, dx=0.4e-6, dy=0.5e-6, z_detector=1.5, detector_size=64 * 0.4e-6,
+                        detector_pixel_size_x=0.4e-6, detector_pixel_size_y=0.5e-6,
+                        wl=prop.convert_energy_wavelength(30000.0), chunk_size=64 * 8, use_fresnel_scaling=True)
+    pf.configure_fresnel_detector(0.0, 1.0)
+    for name, dt in {"c128": np.complex128, "c64": np.complex64}.items():
+        u, U = NV(np.zeros(pf.N, dt)), NV(np.zeros(pf.N, dt))
+        src.PointSource(x=25e-6, y=-40e-6, z=0.0).propagate_to(1.0, pf, 0.8e6, u, U, None)
+        g[f"fp_{name}_u"], g[f"fp_{name}_U"] = u.vec.reshape(48, 64).copy(), U.vec.reshape(48, 64).copy()
+    g["fp_params"] = np.array([64, 48, 0.4e-6, 0.5e-6, 1.0, 25e-6, -40e-6, pf.wl, 0.8e6])
+
     # -- voxel Sample (optical_element.py:502-596): shell, bilinear (pitch != dx), offsets --
     nx = ny = 64
     dx = dy = 0.5e-6

@@ -316,3 +316,30 @@ def test_run_simulation_vs_golden(rs, cuda, golden):
 def test_fast_plan_covers_both_size_families(rs, cuda):
     for n, fast in ((4096, True), (3072, True), (1536, True), (24, True), (40, False), (72, False)):
         assert rs._lib.plan_for(n, 64, cuda).fast is fast
+
+
+def test_fresnel_plane_vs_golden(rs, cuda, golden):
+    """PointSource.propagate_to with Fresnel scaling (big-wave/source.py:62-95)."""
+    nx, ny, dx, dy, dz, xs, ys, wl, f = golden["fp_params"]
+    nx, ny = int(nx), int(ny)
+    p = rs.SimParams(N=nx * ny, nx=nx, ny=ny, dx=dx, dy=dy, z_detector=1.5, detector_size=nx * dx,
+                     detector_pixel_size_x=dx, detector_pixel_size_y=dy, wl=wl, chunk_size=nx * 8,
+                     use_fresnel_scaling=True)
+    p.configure_fresnel_detector(0.0, 1.0)
+    u, U = rs.GpuVector.zeros(nx * ny, cuda), rs.GpuVector.zeros(nx * ny, cuda)
+    rs.PointSource(x=xs, y=ys, z=0.0).propagate_to(dz, p, f, u, U, None)
+    assert rel_l2(host(u, ny, nx), golden["fp_c128_u"]) < 1e-5
+    assert rel_l2(host(U, ny, nx), golden["fp_c128_U"]) < 1e-5
+
+
+@pytest.mark.parametrize("n", [256, 1024])
+def test_fresnel_plane_fast_vs_oracle(rs, cuda, oracle, n):
+    dx = 0.25e-6
+    wl = rs.convert_energy_wavelength(30000.0)
+    p = rs.SimParams(N=n * n, nx=n, ny=n, dx=dx, dy=dx, z_detector=2.0, detector_size=n * dx,
+                     detector_pixel_size_x=dx, detector_pixel_size_y=dx, wl=wl, chunk_size=n, use_fresnel_scaling=True)
+    p.configure_fresnel_detector(0.0, 1.2)
+    u, U = rs.GpuVector.zeros(n * n, cuda), rs.GpuVector.zeros(n * n, cuda)
+    rs.PointSource(x=15e-6, y=7e-6, z=0.0).propagate_to(1.2, p, f := 0.4 / dx, u, U, None)
+    ru, rU = oracle.fresnel_plane_2d(n, n, dx, dx, 1.2, 15e-6, 7e-6, wl, f)
+    assert rel_l2(host(u, n, n), ru) < 1e-5

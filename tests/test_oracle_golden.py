@@ -106,3 +106,12 @@ def test_fastwave_fft_kats(oracle):
     m = np.arange(1, 17, dtype=np.complex128).reshape(4, 4)
     exp4 = np.array([[136, -8 + 8j, -8, -8 - 8j], [-32 + 32j, 0, 0, 0], [-32, 0, 0, 0], [-32 - 32j, 0, 0, 0]])
     np.testing.assert_allclose(oracle.fft2(m), exp4, atol=1e-12)
+
+
+def test_fresnel_plane(golden, oracle):
+    nx, ny, dx, dy, dz, xs, ys, wl, f = golden["fp_params"]
+    for name, dt in (("c128", np.complex128), ("c64", np.complex64)):
+        u, U = oracle.fresnel_plane_2d(int(nx), int(ny), dx, dy, dz, xs, ys, wl, f, dt)
+        tol = 1e-14 if dt == np.complex128 else 1e-6
+        assert rel_l2(u, golden[f"fp_{name}_u"]) < tol
+        assert rel_l2(U, golden[f"fp_{name}_U"]) < tol
