@@ -1,0 +1,180 @@
+"""Gradients of a multislice detector image with respect to per-voxel delta and beta.
+
+The reference has no gradients; this module differentiates the same forward model (per slice:
+bilinear delta+i*beta, transmission exp(-2 pi i t/wl conj(delta + i beta)), Fresnel step with
+the circular cutoff; then free space to the detector and the area_v1 integration of |u|^2).
+
+Adjoint (Wirtinger calculus, g = dL/dconj(u)):
+  detector      g_f = (D^T r) * u_f                      r = dL/dI  (rs_detector_adjoint)
+  Fresnel step  g  = P^H g'   with P^H = step of -dz      (same cutoff mask)
+  transmission  dL/dconj(t) = conj(u) * v,  g = conj(t) * v            (rs_adjoint_slice)
+                dL/ddelta = 4 pi t/wl Im(conj(conj(u) v) t), dL/dbeta = -4 pi t/wl Re(...)
+scattered to the voxels through the bilinear weights. Slice fields are checkpointed every
+`checkpoint_every` slices and recomputed segment by segment on the way back (every slice is
+kept when checkpoint_every is 1).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _lib
+from .propagation import SimParams, propagate_2d, square_and_downsample_2d_device
+from .vector import GpuVector
+
+
+@dataclass
+class VolumeGeometry:
+    """Placement of a (nz, ny_v, nx_v) voxel volume (big-wave/optical_element.py:383-412)."""
+
+    z_start: float
+    pixel_size_x: float
+    pixel_size_y: float
+    pixel_size_z: float
+    x_pos: float = 0.0
+    y_pos: float = 0.0
+
+
+class MultisliceModel:
+    """Detector image I(delta, beta) of a field u0 through a delta/beta voxel volume."""
+
+    def __init__(self, params: SimParams, geom: VolumeGeometry, cutoff: float, u0: torch.Tensor,
+                 checkpoint_every: int | None = None):
+        self.p, self.geom, self.cutoff = params, geom, float(cutoff)
+        self.u0 = u0
+        self.device = u0.device
+        self.checkpoint_every = checkpoint_every
+        n = params.nx * params.ny
+        self.u = GpuVector(torch.empty(n, dtype=torch.complex64, device=self.device))
+        self.U = GpuVector(torch.empty(n, dtype=torch.complex64, device=self.device))
+        self.checkpoints: dict[int, torch.Tensor] = {}
+        self.u_final = None
+
+    # -- helpers ------------------------------------------------------------------------------
+    def _vgeom(self, db: torch.Tensor) -> _lib.VoxelGeom:
+        nz, nyv, nxv, _ = db.shape
+        g = self.geom
+        return _lib.VoxelGeom(nz, nyv, nxv, g.pixel_size_x, g.pixel_size_y, g.pixel_size_z, g.x_pos, g.y_pos)
+
+    def _dz(self, nz: int):
+        return np.full(nz, self.geom.pixel_size_z, dtype=np.float64)
+
+    def _final_dz(self, nz: int) -> float:
+        return self.p.z_detector - (self.geom.z_start + nz * self.geom.pixel_size_z)
+
+    def _step_slices(self, db: torch.Tensor, s0: int, s1: int) -> None:
+        p = self.p
+        plan = _lib.plan_for(p.nx, p.ny, self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().rs_multislice_dbgrid(
+                plan.handle, _lib.ptr(self.u.vec), _lib.ptr(self.U.vec), _lib.ptr(db), self._vgeom(db),
+                float(p.dx), float(p.get_dy()), float(p.wl), self.cutoff, _lib.doubles(self._dz(db.shape[0])), None,
+                s0, s1, _lib.stream_handle()), "rs_multislice_dbgrid")
+
+    # -- forward / backward ---------------------------------------------------------------------
+    def forward(self, db: torch.Tensor) -> torch.Tensor:
+        """float64 detector image; db is (nz, ny_v, nx_v, 2) float32 (delta, beta) on the device."""
+        if db.dtype != torch.float32 or db.dim() != 4 or db.shape[3] != 2 or not db.is_contiguous():
+            raise ValueError("db must be a contiguous (nz, ny_v, nx_v, 2) float32 tensor")
+        nz = db.shape[0]
+        every = self.checkpoint_every or max(1, int(round(math.sqrt(nz))))
+        self.every = every
+        self.u.vec.copy_(self.u0.reshape(-1))
+        self.checkpoints = {}
+        for s0 in range(0, nz, every):
+            self.checkpoints[s0] = self.u.vec.clone()
+            self._step_slices(db, s0, min(nz, s0 + every))
+        p = self.p
+        propagate_2d(self.u, self.U, p.dx, p.get_dy(), p.wl, self._final_dz(nz), p.chunk_size, self.cutoff,
+                     p.nx, p.ny, skip_fft=True)
+        self.u_final = self.u.vec.clone()
+        return square_and_downsample_2d_device(self.u, p, p.z_detector)
+
+    def backward(self, db: torch.Tensor, dI: torch.Tensor) -> torch.Tensor:
+        """dL/d(delta, beta) for the upstream gradient dI = dL/dI of the last forward call."""
+        p = self.p
+        nz = db.shape[0]
+        lib = _lib.lib()
+        plan = _lib.plan_for(p.nx, p.ny, self.device)
+        st = _lib.stream_handle()
+        grad = torch.zeros_like(db)
+        r = dI.to(torch.float64).contiguous()
+        dx, dy = float(p.dx), float(p.get_dy())
+        ds_px, ds_py, det_z, _ = p.effective_detector_geometry(p.z_detector)
+        out_y, out_x = r.shape
+        dgeom = _lib.DetectorGeom(dx, dy, ds_px, ds_py, det_z, out_x, out_y,
+                                  0 if p.detector_integrator == "area_v1" else 1, 0)
+        g = GpuVector(torch.empty_like(self.u.vec))
+        scratch = GpuVector(torch.empty_like(self.u.vec))
+        with torch.cuda.device(self.device):
+            _lib.check(lib.rs_detector_adjoint(plan.handle, _lib.ptr(self.u_final), _lib.ptr(g.vec), _lib.ptr(r),
+                                               dgeom, st), "rs_detector_adjoint")
+        # P_final^H
+        propagate_2d(g, scratch, p.dx, p.get_dy(), p.wl, -self._final_dz(nz), p.chunk_size, self.cutoff, p.nx, p.ny)
+        vg = self._vgeom(db)
+        for s0 in sorted(self.checkpoints, reverse=True):
+            s1 = min(nz, s0 + self.every)
+            # recompute the fields entering slices s0 .. s1-1 from the checkpoint
+            self.u.vec.copy_(self.checkpoints[s0])
+            fields = []
+            for k in range(s0, s1):
+                fields.append(self.u.vec.clone())
+                if k + 1 < s1:
+                    self._step_slices(db, k, k + 1)
+            for k in range(s1 - 1, s0 - 1, -1):
+                propagate_2d(g, scratch, p.dx, p.get_dy(), p.wl, -self.geom.pixel_size_z, p.chunk_size, self.cutoff,
+                             p.nx, p.ny)
+                with torch.cuda.device(self.device):
+                    _lib.check(lib.rs_adjoint_slice(plan.handle, _lib.ptr(g.vec), _lib.ptr(fields[k - s0]),
+                                                    _lib.ptr(db), vg, dx, dy, float(p.wl), k, 1.0, _lib.ptr(grad), st),
+                               "rs_adjoint_slice")
+        return grad
+
+
+class _MultisliceIntensity(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, db: torch.Tensor, model: MultisliceModel) -> torch.Tensor:
+        ctx.model = model
+        ctx.save_for_backward(db)
+        return model.forward(db.detach().contiguous())
+
+    @staticmethod
+    def backward(ctx, dI: torch.Tensor):
+        (db,) = ctx.saved_tensors
+        return ctx.model.backward(db.detach().contiguous(), dI), None
+
+
+def multislice_intensity(db: torch.Tensor, model: MultisliceModel) -> torch.Tensor:
+    """Differentiable detector image: torch.autograd sees dI/d(db) through the hand-written adjoint."""
+    return _MultisliceIntensity.apply(db, model)
+
+
+def gaussian_plasma_db(n0: torch.Tensor, length: torch.Tensor, te: torch.Tensor, shape: tuple[int, int, int],
+                       pitch: tuple[float, float, float], energy: float, zstar: float = 3.5, z2bar: float = 18.5,
+                       zbar: float = 3.5) -> torch.Tensor:
+    """(nz, ny_v, nx_v, 2) float32 delta/beta of n_e = n0 exp(-r^2/2L^2), n_i = n_e/Z*, uniform T_e, in
+    torch (so n0, L, T_e receive gradients): delta = r_e lambda^2/(2 pi) n_e and the Kramers beta of
+    big-wave/plasma.py:380-434 with q = Z*/zbar = 1 (no bound electrons)."""
+    import scipy.constants as consts
+    planck_hc = 1.e10 * consts.Planck * consts.c / consts.e
+    r_e = 100.0 * consts.physical_constants["classical electron radius"][0]
+    dev = n0.device
+    nz, ny, nx = shape
+    pz, py, px = pitch
+    z = (torch.arange(nz, device=dev, dtype=torch.float64) + 0.5 - nz / 2.0) * pz
+    y = (torch.arange(ny, device=dev, dtype=torch.float64) - ny / 2.0) * py
+    x = (torch.arange(nx, device=dev, dtype=torch.float64) - nx / 2.0) * px
+    r2 = z[:, None, None] ** 2 + y[None, :, None] ** 2 + x[None, None, :] ** 2
+    ne = n0 * torch.exp(-r2 / (2.0 * length ** 2))
+    ni = ne / zstar
+    lamb_cm = 1.0e-8 * planck_hc / energy
+    pref = r_e * lamb_cm * lamb_cm / (2.0 * math.pi)
+    q = min(max(zstar / zbar, 0.0), 1.0)
+    nu = energy / 4.135667e-15
+    delta = ne * pref
+    alpha = 3.7e8 * ne * ni * (q * q * z2bar) / (torch.sqrt(te * 11604.5) * nu ** 3)
+    beta = alpha * lamb_cm / (4.0 * math.pi)
+    return torch.stack([delta, beta], dim=-1).to(torch.float32).contiguous()

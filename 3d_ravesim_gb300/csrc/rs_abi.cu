@@ -73,13 +73,17 @@ struct rs_plan {
   int nx = 0, ny = 0, dev = 0;
   bool fast = false;
   void* arena = nullptr;
-  float2* tw_x = nullptr;
+  float4* tws_x = nullptr;  // compensated stage-major twiddles (fast sizes)
+  float4* tws_y = nullptr;
+  float4* tw2_y = nullptr;  // two-level column-transform table (power-of-two ny >= 256)
+  float2* tw_x = nullptr;   // plain twiddles of the direct-DFT path (other sizes)
   float2* tw_y = nullptr;
   float2* ex = nullptr;
   float2* ey = nullptr;
   int* ylim = nullptr;
   int* xi = nullptr;
   float* xf = nullptr;
+  int2* xp = nullptr;
   int* yi = nullptr;
   float* yf = nullptr;
   void* det = nullptr;
@@ -138,14 +142,14 @@ int build_prop(rs_plan* p, double dx, double dy, double wl, double dz, double cu
 }
 
 int build_axes(rs_plan* p, const rs_voxel_geom* g, double dx, double dy, double cs, cudaStream_t s) {
-  AxisTabArgs ax{p->nx, dx, cs, g->x_pos, g->nx_v, g->pixel_size_x, p->xi, p->xf};
+  AxisTabArgs ax{p->nx, dx, cs, g->x_pos, g->nx_v, g->pixel_size_x, p->xi, p->xf, p->xp};
   RS_CK(launch_axis_table(ax, s));
-  AxisTabArgs ay{p->ny, dy, cs, g->y_pos, g->ny_v, g->pixel_size_y, p->yi, p->yf};
+  AxisTabArgs ay{p->ny, dy, cs, g->y_pos, g->ny_v, g->pixel_size_y, p->yi, p->yf, nullptr};
   RS_CK(launch_axis_table(ay, s));
   return RS_OK;
 }
 
-AxisTab axis_tab(const rs_plan* p) { return AxisTab{p->xi, p->xf, p->yi, p->yf}; }
+AxisTab axis_tab(const rs_plan* p) { return AxisTab{p->xi, p->xf, p->yi, p->yf, p->xp}; }
 
 // ---- pipelined passes -------------------------------------------------------------------
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
@@ -192,7 +196,9 @@ cudaError_t run_row(rs_plan* p, const RowArgs& r, cudaStream_t s) {
   return launch_row_pass(p->nx, r, s);
 }
 
-cudaError_t run_col(rs_plan* p, const ColArgs& c, cudaStream_t s) {
+cudaError_t run_col(rs_plan* p, const ColArgs& ca, cudaStream_t s) {
+  ColArgs c = ca;
+  c.tw2 = p->tw2_y;
   int w = 0, bh = 0;
   if (p->pipe_cols && col_pipe_box(p->ny, &w, &bh) && aligned16(c.in) && aligned16(c.out) && tensor_map_encoder()) {
     // Copy the input map before the output lookup: encoding the output may recycle its slot.
@@ -231,10 +237,10 @@ void prof_end(rs_plan* p, int idx, cudaStream_t s) {
 int fft2_impl(rs_plan* p, const float2* in, float2* out, cudaStream_t s) {
   if (p->fast) {
     RowArgs r{};
-    r.in = in; r.out = out; r.ny = p->ny; r.flags = ROW_FWD; r.tw = p->tw_x;
+    r.in = in; r.out = out; r.ny = p->ny; r.flags = ROW_FWD; r.tw = p->tws_x;
     RS_CK(run_row(p, r, s));
     ColArgs c{};
-    c.in = out; c.out = out; c.nx = p->nx; c.flags = COL_FWD; c.tw = p->tw_y;
+    c.in = out; c.out = out; c.nx = p->nx; c.flags = COL_FWD; c.tw = p->tws_y;
     RS_CK(run_col(p, c, s));
   } else {
     RS_CK(launch_dft_axis(in, out, p->nx, p->ny, 0, 0, p->tw_x, 1.0f, s));
@@ -247,10 +253,10 @@ int ifft2_impl(rs_plan* p, const float2* in, float2* out, cudaStream_t s) {
   const float inv_n = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
   if (p->fast) {
     ColArgs c{};
-    c.in = in; c.out = out; c.nx = p->nx; c.flags = COL_INV | COL_SCALE; c.scale = inv_n; c.tw = p->tw_y;
+    c.in = in; c.out = out; c.nx = p->nx; c.flags = COL_INV | COL_SCALE; c.scale = inv_n; c.tw = p->tws_y;
     RS_CK(run_col(p, c, s));
     RowArgs r{};
-    r.in = out; r.out = out; r.ny = p->ny; r.flags = ROW_INV; r.tw = p->tw_x;
+    r.in = out; r.out = out; r.ny = p->ny; r.flags = ROW_INV; r.tw = p->tws_x;
     RS_CK(run_row(p, r, s));
   } else {
     RS_CK(launch_dft_axis(in, out, p->nx, p->ny, 1, 1, p->tw_y, 1.0f, s));
@@ -274,6 +280,7 @@ struct SliceSource {
   // exactly one of vox / pl is used
   bool plasma = false;
   const char* grid = nullptr;  // voxel ids
+  const float2* dbv = nullptr; // or (delta, beta) per voxel
   int grid_signed = 0;
   const float2* db = nullptr;
   int n_db = 0;
@@ -316,7 +323,8 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
     VoxelArgs vox{};
     PlasmaArgs pl{};
     if (!src.plasma) {
-      vox.slice = src.grid + plane * z * 4;
+      vox.slice = src.grid ? src.grid + plane * z * 4 : nullptr;
+      vox.dbv = src.dbv ? src.dbv + plane * z : nullptr;
       vox.grid_signed = src.grid_signed;
       vox.nxv = g->nx_v;
       vox.nyv = g->ny_v;
@@ -337,7 +345,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
     }
     if (p->fast) {
       RowArgs r{};
-      r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tw_x; r.ax = axis_tab(p);
+      r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tws_x; r.ax = axis_tab(p);
       r.flags = (z == s0 ? 0 : ROW_INV) | ROW_FWD | (src.plasma ? ROW_TPLASMA : ROW_TVOX);
       r.vox = vox;
       r.pl = pl;
@@ -345,7 +353,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       RS_CK(run_row(p, r, s));
       prof_end(p, er, s);
       ColArgs c{};
-      c.in = u; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_y;
+      c.in = u; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tws_y;
       c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
       c.flags = COL_FWD | COL_H | COL_SCALE | COL_INV | (z == s1 - 1 ? COL_SPEC : 0);
       const int ec = prof_begin(p, 1, s);
@@ -357,7 +365,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
   }
   if (p->fast) {
     RowArgs r{};
-    r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tw_x; r.flags = ROW_INV;
+    r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tws_x; r.flags = ROW_INV;
     RS_CK(run_row(p, r, s));
   }
   return RS_OK;
@@ -489,28 +497,42 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   p->fast = fast;
   cudaError_t e = cudaGetDevice(&p->dev);
   if (e != cudaSuccess) { delete p; return fail(RS_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e)); }
-  // arena: tw_x (twx entries), ex (nx) | tw_y (twy), ey (ny) | ylim, xi (nx int) | xf (nx) | yi (ny) | yf (ny)
-  const bool stage_tw = fast && RS_TW_STAGE_MAJOR;
-  const size_t twx = stage_tw ? std::max(stage_twiddle_len(nx), 1) : nx;
-  const size_t twy = stage_tw ? std::max(stage_twiddle_len(ny), 1) : ny;
-  const size_t bytes = align8(sizeof(float2) * (twx + nx)) + align8(sizeof(float2) * (twy + ny)) +
-                       align8(sizeof(int) * 2 * nx) + align8(sizeof(float) * nx) +
-                       align8(sizeof(int) * ny) + align8(sizeof(float) * ny) + 8;
+  // One arena per plan. Fast sizes: compensated stage-major twiddles per axis (float4) and the
+  // two-level column table; other sizes: plain twiddles per axis (float2) for the direct DFT.
+  // Then ex, ey, ylim, the sample-coordinate tables and the status word.
+  const size_t twx = fast ? std::max(stage_twiddle_len(nx), 1) : 0;
+  const size_t twy = fast ? std::max(stage_twiddle_len(ny), 1) : 0;
+  const size_t tw2y = fast ? static_cast<size_t>(twiddles_2l_len(ny)) : 0;
+  const size_t gx = fast ? 0 : nx, gy = fast ? 0 : ny;
+  size_t bytes = 0;
+  auto take = [&](size_t n) { const size_t at = bytes; bytes += (n + 15) & ~static_cast<size_t>(15); return at; };
+  const size_t o_twx = take(sizeof(float4) * twx), o_twy = take(sizeof(float4) * twy);
+  const size_t o_tw2y = take(sizeof(float4) * tw2y);
+  const size_t o_gx = take(sizeof(float2) * gx), o_gy = take(sizeof(float2) * gy);
+  const size_t o_ex = take(sizeof(float2) * nx), o_ey = take(sizeof(float2) * ny);
+  const size_t o_ylim = take(sizeof(int) * nx), o_xi = take(sizeof(int) * nx), o_xf = take(sizeof(float) * nx);
+  const size_t o_yi = take(sizeof(int) * ny), o_yf = take(sizeof(float) * ny), o_xp = take(sizeof(int2) * nx);
+  const size_t o_status = take(sizeof(int));
   e = cudaMalloc(&p->arena, bytes);
   if (e != cudaSuccess) { delete p; return fail(RS_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
   char* c = static_cast<char*>(p->arena);
-  p->tw_x = reinterpret_cast<float2*>(c);
-  p->ex = p->tw_x + twx;
-  c += align8(sizeof(float2) * (twx + nx));
-  p->tw_y = reinterpret_cast<float2*>(c);
-  p->ey = p->tw_y + twy;
-  c += align8(sizeof(float2) * (twy + ny));
-  p->ylim = reinterpret_cast<int*>(c); c += align8(sizeof(int) * nx);
-  p->xi = reinterpret_cast<int*>(c); c += align8(sizeof(int) * nx);
-  p->xf = reinterpret_cast<float*>(c); c += align8(sizeof(float) * nx);
-  p->yi = reinterpret_cast<int*>(c); c += align8(sizeof(int) * ny);
-  p->yf = reinterpret_cast<float*>(c); c += align8(sizeof(float) * ny);
-  p->status = reinterpret_cast<int*>(c);
+  if (fast) {
+    p->tws_x = reinterpret_cast<float4*>(c + o_twx);
+    p->tws_y = reinterpret_cast<float4*>(c + o_twy);
+    if (tw2y) p->tw2_y = reinterpret_cast<float4*>(c + o_tw2y);
+  } else {
+    p->tw_x = reinterpret_cast<float2*>(c + o_gx);
+    p->tw_y = reinterpret_cast<float2*>(c + o_gy);
+  }
+  p->ex = reinterpret_cast<float2*>(c + o_ex);
+  p->ey = reinterpret_cast<float2*>(c + o_ey);
+  p->ylim = reinterpret_cast<int*>(c + o_ylim);
+  p->xi = reinterpret_cast<int*>(c + o_xi);
+  p->xf = reinterpret_cast<float*>(c + o_xf);
+  p->yi = reinterpret_cast<int*>(c + o_yi);
+  p->yf = reinterpret_cast<float*>(c + o_yf);
+  p->xp = reinterpret_cast<int2*>(c + o_xp);
+  p->status = reinterpret_cast<int*>(c + o_status);
   // RS_PIPELINE: unset -> default; "0" none; "1" both; "rows" / "cols" one direction
   const char* env = std::getenv("RS_PIPELINE");
   p->pipe_rows = kDefaultPipeRows;
@@ -520,8 +542,9 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
     p->pipe_rows = v == "1" || v == "rows";
     p->pipe_cols = v == "1" || v == "cols";
   }
-  e = stage_tw ? launch_stage_twiddles(nx, p->tw_x, 0) : launch_twiddles(p->tw_x, nx, 0);
-  if (e == cudaSuccess) e = stage_tw ? launch_stage_twiddles(ny, p->tw_y, 0) : launch_twiddles(p->tw_y, ny, 0);
+  e = fast ? launch_stage_twiddles(nx, p->tws_x, 0) : launch_twiddles(p->tw_x, nx, 0);
+  if (e == cudaSuccess) e = fast ? launch_stage_twiddles(ny, p->tws_y, 0) : launch_twiddles(p->tw_y, ny, 0);
+  if (e == cudaSuccess && p->tw2_y) e = launch_twiddles_2l(ny, p->tw2_y, 0);
   if (e == cudaSuccess) e = cudaMemsetAsync(p->status, 0, sizeof(int), 0);
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   if (e != cudaSuccess) {
@@ -638,16 +661,16 @@ int rs_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double wl
     const float inv_n = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
     if (!skip_fft) {
       RowArgs r{};
-      r.in = u; r.out = U; r.ny = p->ny; r.flags = ROW_FWD; r.tw = p->tw_x;
+      r.in = u; r.out = U; r.ny = p->ny; r.flags = ROW_FWD; r.tw = p->tws_x;
       RS_CK(run_row(p, r, s));
     }
     ColArgs c{};
-    c.in = U; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_y;
+    c.in = U; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tws_y;
     c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
     c.flags = (skip_fft ? 0 : COL_FWD) | COL_H | COL_SPEC | COL_SCALE | COL_INV;
     RS_CK(run_col(p, c, s));
     RowArgs r{};
-    r.in = u; r.out = u; r.ny = p->ny; r.flags = ROW_INV; r.tw = p->tw_x;
+    r.in = u; r.out = u; r.ny = p->ny; r.flags = ROW_INV; r.tw = p->tws_x;
     RS_CK(run_row(p, r, s));
   } else {
     if (!skip_fft) RS_TRY(fft2_impl(p, u, U, s));
@@ -725,15 +748,15 @@ static int source_propagate(rs_plan* p, void* u_, void* U_, const PointSrcArgs& 
   RS_TRY(build_prop(p, dx, dy, wl, 0.0, cutoff, false, s));
   if (p->fast) {
     RowArgs r{};
-    r.out = U; r.ny = p->ny; r.flags = ROW_SRC | ROW_FWD; r.tw = p->tw_x; r.ps = a;
+    r.out = U; r.ny = p->ny; r.flags = ROW_SRC | ROW_FWD; r.tw = p->tws_x; r.ps = a;
     RS_CK(run_row(p, r, s));
     ColArgs c{};
-    c.in = U; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_y; c.ylim = p->ylim;
+    c.in = U; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tws_y; c.ylim = p->ylim;
     c.scale = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
     c.flags = COL_FWD | COL_MASK | COL_SPEC | COL_SCALE | COL_INV;
     RS_CK(run_col(p, c, s));
     RowArgs r2{};
-    r2.in = u; r2.out = u; r2.ny = p->ny; r2.flags = ROW_INV; r2.tw = p->tw_x;
+    r2.in = u; r2.out = u; r2.ny = p->ny; r2.flags = ROW_INV; r2.tw = p->tws_x;
     RS_CK(run_row(p, r2, s));
   } else {
     RS_CK(launch_point_source(u, p->nx, p->ny, a, s));
@@ -780,15 +803,141 @@ int rs_multislice_plasma(rs_plan* p, void* u, void* U, const void* ne, const voi
   const double pref = pc->r_electron_cm * lamb_cm * lamb_cm / (2.0 * M_PI);
   const double nu = pc->energy_ev / 4.135667e-15;
   PlasmaArgs& b = src.pl_base;
-  b.pref = pref;
-  b.f1bar = pc->f1bar;
-  b.f2eff = pc->f2eff_bar;
-  b.zbar_pos = pc->zbar > 0.0 ? 1.0 : 0.0;
-  b.inv_zbar = pc->zbar > 0.0 ? 1.0 / pc->zbar : 0.0;
-  b.z2bar_pos = pc->z2bar > 0.0 ? 1.0 : 0.0;
-  b.cff = 3.7e8 * pc->z2bar / (std::sqrt(11604.5) * nu * nu * nu) * lamb_cm / (4.0 * M_PI) * 1e40;
+  b.pref20 = static_cast<float>(pref * 1e20);
+  b.f1bar = static_cast<float>(pc->f1bar);
+  b.f2eff = static_cast<float>(pc->f2eff_bar);
+  b.zbar_pos = pc->zbar > 0.0 ? 1 : 0;
+  b.inv_zbar = pc->zbar > 0.0 ? static_cast<float>(1.0 / pc->zbar) : 0.0f;
+  b.z2bar_pos = pc->z2bar > 0.0 ? 1 : 0;
+  b.cff = static_cast<float>(3.7e8 * pc->z2bar / (std::sqrt(11604.5) * nu * nu * nu) * lamb_cm / (4.0 * M_PI) * 1e40);
   return multislice(p, static_cast<float2*>(u), static_cast<float2*>(U), src, geom, dx, dy, wl, cutoff,
                     slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
+}
+
+int rs_multislice_dbgrid(rs_plan* p, void* u, void* U, const float* db_grid, const rs_voxel_geom* geom,
+                         double dx, double dy, double wl, double cutoff, const double* slice_dz,
+                         const double* coord_scale, int slice_begin, int slice_end, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!db_grid) return fail(RS_EINVAL, "db_grid must be a device pointer");
+  SliceSource src;
+  src.dbv = reinterpret_cast<const float2*>(db_grid);
+  src.n_db = 1;
+  return multislice(p, static_cast<float2*>(u), static_cast<float2*>(U), src, geom, dx, dy, wl, cutoff,
+                    slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
+}
+
+int rs_adjoint_slice(rs_plan* p, void* v, const void* u, const float* db_grid, const rs_voxel_geom* g,
+                     double dx, double dy, double wl, int slice, double coord_scale, float* grad_grid,
+                     void* stream) {
+  RS_TRY(check_plan(p));
+  if (!v || !u || !db_grid || !grad_grid || !g) return fail(RS_EINVAL, "NULL pointer argument");
+  if (slice < 0 || slice >= g->nz) return fail(RS_EINVAL, "slice %d outside [0, %d)", slice, g->nz);
+  if (g->ny_v < 2 || g->nx_v < 2) return fail(RS_EINVAL, "bad grid shape");
+  if (!finite_pos(wl)) return fail(RS_EINVAL, "wavelength must be positive");
+  if (static_cast<size_t>(g->nx_v) * 16 > 200 * 1024) return fail(RS_EUNSUPPORTED, "voxel rows wider than 12800");
+  cudaStream_t s = as_stream(stream);
+  RS_TRY(build_axes(p, g, dx, dy, coord_scale, s));
+  const size_t plane = static_cast<size_t>(g->ny_v) * g->nx_v;
+  AdjointSliceArgs a{};
+  a.v = static_cast<float2*>(v);
+  a.u = static_cast<const float2*>(u);
+  a.dbv = reinterpret_cast<const float2*>(db_grid) + plane * slice;
+  a.grad = reinterpret_cast<float2*>(grad_grid) + plane * slice;
+  a.nx = p->nx;
+  a.ny = p->ny;
+  a.nxv = g->nx_v;
+  a.nyv = g->ny_v;
+  a.ax = axis_tab(p);
+  a.a = static_cast<float>(g->pixel_size_z / wl);
+  RS_CK(launch_adjoint_slice(a, s));
+  return RS_OK;
+}
+
+int rs_detector_adjoint(rs_plan* p, const void* u, void* g_out, const double* r, const rs_detector_geom* g,
+                        void* stream) {
+  RS_TRY(check_plan(p));
+  if (!u || !g_out || !r || !g) return fail(RS_EINVAL, "NULL pointer argument");
+  if (g->out_x <= 0 || g->out_y <= 0) return fail(RS_EINVAL, "detector output must be non-empty");
+  if (!finite_pos(g->dx) || !finite_pos(g->dy) || !finite_pos(g->ds_px) || !finite_pos(g->ds_py))
+    return fail(RS_EINVAL, "detector and grid spacings must be positive");
+  if (!std::isfinite(g->detector_z) || g->detector_z == 0.0) return fail(RS_EINVAL, "detector z must be finite and non-zero");
+  DetTables t;
+  if (g->integrator == 0) build_area_v1(p->nx, p->ny, *g, t);
+  else if (g->integrator == 1) build_legacy(p->nx, p->ny, *g, t);
+  else return fail(RS_EINVAL, "unknown integrator %d", g->integrator);
+  // invert the per-detector-pixel lists into per-grid-cell lists
+  std::vector<int> xptr(p->nx + 1, 0), yptr(p->ny + 1, 0);
+  for (int c : t.xcell) ++xptr[c + 1];
+  for (int c : t.ycell) ++yptr[c + 1];
+  for (int i = 0; i < p->nx; ++i) xptr[i + 1] += xptr[i];
+  for (int i = 0; i < p->ny; ++i) yptr[i + 1] += yptr[i];
+  std::vector<int> xdet(t.xcell.size()), ydet(t.ycell.size());
+  std::vector<float> xw(t.xcell.size());
+  std::vector<double> yw(t.ycell.size());
+  {
+    std::vector<int> fill(xptr.begin(), xptr.end() - 1);
+    for (int o = 0; o < g->out_x; ++o)
+      for (int k = t.xptr[o]; k < t.xptr[o + 1]; ++k) {
+        const int pos = fill[t.xcell[k]]++;
+        xdet[pos] = o;
+        xw[pos] = t.xw[k];
+      }
+    std::vector<int> filly(yptr.begin(), yptr.end() - 1);
+    for (int o = 0; o < g->out_y; ++o)
+      for (int k = t.yptr[o]; k < t.yptr[o + 1]; ++k) {
+        const int pos = filly[t.ycell[k]]++;
+        ydet[pos] = o;
+        yw[pos] = t.yw[k];
+      }
+  }
+  const size_t o_xpos = 0;
+  const size_t o_ypos = o_xpos + align8(t.xdet.size() * 8);
+  const size_t o_yw = o_ypos + align8(t.ydet.size() * 8);
+  const size_t o_xw = o_yw + align8(yw.size() * 8);
+  const size_t o_xptr = o_xw + align8(xw.size() * 4);
+  const size_t o_xdet = o_xptr + align8(xptr.size() * 4);
+  const size_t o_yptr = o_xdet + align8(xdet.size() * 4);
+  const size_t o_ydet = o_yptr + align8(yptr.size() * 4);
+  const size_t total = o_ydet + align8(ydet.size() * 4) + 8;
+  std::vector<char> host(total, 0);
+  auto put = [&](size_t off, const void* src, size_t n) { if (n) std::memcpy(host.data() + off, src, n); };
+  put(o_xpos, t.xdet.data(), t.xdet.size() * 8);
+  put(o_ypos, t.ydet.data(), t.ydet.size() * 8);
+  put(o_yw, yw.data(), yw.size() * 8);
+  put(o_xw, xw.data(), xw.size() * 4);
+  put(o_xptr, xptr.data(), xptr.size() * 4);
+  put(o_xdet, xdet.data(), xdet.size() * 4);
+  put(o_yptr, yptr.data(), yptr.size() * 4);
+  put(o_ydet, ydet.data(), ydet.size() * 4);
+  cudaStream_t s = as_stream(stream);
+  if (total > p->det_cap) {
+    if (p->det) RS_CK(cudaFree(p->det));
+    p->det = nullptr;
+    p->det_cap = 0;
+    cudaError_t e = cudaMalloc(&p->det, total);
+    if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc(%zu) for detector tables: %s", total, cudaGetErrorString(e));
+    p->det_cap = total;
+  }
+  char* d = static_cast<char*>(p->det);
+  RS_CK(cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, s));
+  DetAdjArgs a{};
+  a.u = static_cast<const float2*>(u);
+  a.g = static_cast<float2*>(g_out);
+  a.r = r;
+  a.nx = p->nx;
+  a.ny = p->ny;
+  a.out_x = g->out_x;
+  a.xpos = reinterpret_cast<const double*>(d + o_xpos);
+  a.ypos = reinterpret_cast<const double*>(d + o_ypos);
+  a.yw = reinterpret_cast<const double*>(d + o_yw);
+  a.xw = reinterpret_cast<const float*>(d + o_xw);
+  a.xptr = reinterpret_cast<const int*>(d + o_xptr);
+  a.xdet = reinterpret_cast<const int*>(d + o_xdet);
+  a.yptr = reinterpret_cast<const int*>(d + o_yptr);
+  a.ydet = reinterpret_cast<const int*>(d + o_ydet);
+  a.z = g->detector_z;
+  RS_CK(launch_detector_adjoint(a, s));
+  return RS_OK;
 }
 
 int rs_apply_transmission_voxel(rs_plan* p, void* u, const void* grid, int grid_signed, const float* db,

@@ -32,16 +32,40 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
 }
+
+// Compensated twiddles. A twiddle rounded to float carries the same relative error (~3e-8)
+// into every transform of every slice, so over hundreds of slice-steps those errors add up
+// coherently (to ~1e-4 after 512 slices). A twiddle is therefore stored as w = hi + lo
+// (float4 {hi.x, hi.y, lo.x, lo.y}, lo the float nearest to the FP64 rounding residual,
+// hi + lo exact to ~2^-48) and a * w is formed as a*lo + a*hi, the small product first, so
+// that only the final roundings, which depend on a, remain.
+__device__ __forceinline__ float2 cmul_tw(float2 a, float4 w) {
+  const float cr = fmaf(a.x, w.z, -a.y * w.w);
+  const float ci = fmaf(a.x, w.w, a.y * w.z);
+  return make_float2(fmaf(a.x, w.x, fmaf(-a.y, w.y, cr)), fmaf(a.x, w.y, fmaf(a.y, w.x, ci)));
+}
+// a * conj(w)
+__device__ __forceinline__ float2 cmulc_tw(float2 a, float4 w) {
+  const float cr = fmaf(a.x, w.z, a.y * w.w);
+  const float ci = fmaf(a.y, w.z, -a.x * w.w);
+  return make_float2(fmaf(a.x, w.x, fmaf(a.y, w.y, cr)), fmaf(a.y, w.x, fmaf(-a.x, w.y, ci)));
+}
+// x * (hi + lo) for a real constant split the same way
+__device__ __forceinline__ float mulk(float x, float hi, float lo) { return fmaf(hi, x, lo * x); }
 // multiply by -i (forward) or +i (inverse)
 template <bool INV>
 __device__ __forceinline__ float2 mul_mi(float2 a) {
   return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
 }
 
-// cos(pi/8), sin(pi/8), sqrt(2)/2 (mathematical constants, correctly rounded to float).
+// cos(pi/8), sin(pi/8), sqrt(2)/2 (mathematical constants, correctly rounded to float), and
+// the floats nearest to their rounding residuals (constant - float(constant)).
 constexpr float kC8 = 0.92387953251128675613f;
 constexpr float kS8 = 0.38268343236508977173f;
 constexpr float kR2 = 0.70710678118654752440f;
+constexpr float kC8lo = 2.830748968563057e-08f;
+constexpr float kS8lo = 6.2233507236442165e-09f;
+constexpr float kR2lo = 1.2101617485882343e-08f;
 
 // Multiply by W16^m = exp(-+2*pi*i*m/16) for the m used inside the 4x4 radix-16 butterfly.
 template <int M, bool INV>
@@ -52,18 +76,21 @@ __device__ __forceinline__ float2 tw16(float2 a) {
     return mul_mi<INV>(a);
   } else if constexpr (M == 2) {
     // fwd: c(1 - i); inv: c(1 + i)
-    return INV ? make_float2(kR2 * (a.x - a.y), kR2 * (a.x + a.y))
-               : make_float2(kR2 * (a.x + a.y), kR2 * (a.y - a.x));
+    return INV ? make_float2(mulk(a.x - a.y, kR2, kR2lo), mulk(a.x + a.y, kR2, kR2lo))
+               : make_float2(mulk(a.x + a.y, kR2, kR2lo), mulk(a.y - a.x, kR2, kR2lo));
   } else if constexpr (M == 6) {
     // fwd: c(-1 - i); inv: c(-1 + i)
-    return INV ? make_float2(-kR2 * (a.x + a.y), kR2 * (a.x - a.y))
-               : make_float2(kR2 * (a.y - a.x), -kR2 * (a.x + a.y));
+    return INV ? make_float2(-mulk(a.x + a.y, kR2, kR2lo), mulk(a.x - a.y, kR2, kR2lo))
+               : make_float2(mulk(a.y - a.x, kR2, kR2lo), -mulk(a.x + a.y, kR2, kR2lo));
   } else {
     // generic: M in {1, 3, 9}
     constexpr float wr = (M == 1) ? kC8 : (M == 3) ? kS8 : -kC8;
     constexpr float wi0 = (M == 1) ? -kS8 : (M == 3) ? -kC8 : kS8;  // forward imaginary part
+    constexpr float wrl = (M == 1) ? kC8lo : (M == 3) ? kS8lo : -kC8lo;
+    constexpr float wil0 = (M == 1) ? -kS8lo : (M == 3) ? -kC8lo : kS8lo;
     constexpr float wi = INV ? -wi0 : wi0;
-    return cmul(a, make_float2(wr, wi));
+    constexpr float wil = INV ? -wil0 : wil0;
+    return cmul_tw(a, make_float4(wr, wi, wrl, wil));
   }
 }
 
@@ -129,13 +156,15 @@ __device__ __forceinline__ void dft16(float2 (&a)[16]) {
 
 // 3-point DFT: y0 = a0 + t, y1,2 = a0 - t/2 -+ i*(sqrt(3)/2)*(a1 - a2) (forward), t = a1 + a2.
 constexpr float kHalfSqrt3 = 0.86602540378443864676f;
+constexpr float kHalfSqrt3lo = 1.5543625053737742e-08f;
 
 template <bool INV>
 __device__ __forceinline__ void dft3(float2& a0, float2& a1, float2& a2) {
   const float2 t = cadd(a1, a2);
   const float2 d = csub(a1, a2);
   const float2 m = make_float2(fmaf(-0.5f, t.x, a0.x), fmaf(-0.5f, t.y, a0.y));
-  const float2 q = cscale(mul_mi<INV>(d), kHalfSqrt3);
+  const float2 md = mul_mi<INV>(d);
+  const float2 q = make_float2(mulk(md.x, kHalfSqrt3, kHalfSqrt3lo), mulk(md.y, kHalfSqrt3, kHalfSqrt3lo));
   a0 = cadd(a0, t);
   a1 = cadd(m, q);
   a2 = csub(m, q);

@@ -19,11 +19,16 @@ cudaError_t launch_col_pass(int ny, const ColArgs& a, cudaStream_t s) {
   return is_pow2(ny) ? launch_col_pass_pow2(ny, a, s) : launch_col_pass_pow3(ny, a, s);
 }
 
-cudaError_t launch_stage_twiddles(int n, float2* tw, cudaStream_t s) {
+cudaError_t launch_stage_twiddles(int n, float4* tw, cudaStream_t s) {
   return is_pow2(n) ? launch_stage_twiddles_pow2(n, tw, s) : launch_stage_twiddles_pow3(n, tw, s);
 }
 
 int stage_twiddle_len(int n) { return is_pow2(n) ? stage_twiddle_len_pow2(n) : stage_twiddle_len_pow3(n); }
+
+int twiddles_2l_len(int n) { return is_pow2(n) ? twiddles_2l_len_pow2(n) : 0; }
+cudaError_t launch_twiddles_2l(int n, float4* tw, cudaStream_t s) {
+  return is_pow2(n) ? launch_twiddles_2l_pow2(n, tw, s) : cudaErrorInvalidValue;
+}
 
 bool row_pipe_ok(int n) { return is_pow2(n) ? row_pipe_ok_pow2(n) : row_pipe_ok_pow3(n); }
 bool col_pipe_box(int n, int* w, int* bh) { return is_pow2(n) ? col_pipe_box_pow2(n, w, bh) : col_pipe_box_pow3(n, w, bh); }

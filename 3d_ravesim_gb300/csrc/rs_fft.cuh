@@ -21,9 +21,6 @@
 #include <utility>
 #include "rs_common.cuh"
 
-#ifndef RS_TW_STAGE_MAJOR
-#define RS_TW_STAGE_MAJOR 1
-#endif
 
 namespace rs {
 
@@ -83,6 +80,10 @@ struct PadAddr {
 struct SwzAddr {
   static __device__ __forceinline__ int at(int p) { return p ^ ((p >> 4) & 15); }
 };
+// NatAddr: natural order (the layout bulk copies fill and drain).
+struct NatAddr {
+  static __device__ __forceinline__ int at(int p) { return p; }
+};
 
 // Position held by register e of thread t in a radix-R mapping.
 template <int N, int R>
@@ -98,17 +99,20 @@ __device__ __forceinline__ void dft_all(float2 (&v)[E], std::integer_sequence<in
 // Twiddle-load policies: from global memory through the read-only path, or from a copy of the
 // table in shared memory (a generic pointer into the block's shared window).
 struct TwGlobal {
-  static __device__ __forceinline__ float2 load(const float2* p) { return __ldg(p); }
+  static __device__ __forceinline__ float4 load(const float4* p) { return __ldg(p); }
 };
 struct TwShared {
-  static __device__ __forceinline__ float2 load(const float2* p) { return *p; }
+  static __device__ __forceinline__ float4 load(const float4* p) { return *p; }
 };
 
-template <int N, bool INV, int SI, int NS, class AD = PadAddr, int STR = 1, class TWL = TwGlobal>
+// WARP = false: the sequence spans the block; each exchange is write, barrier, read, barrier.
+// WARP = true : the sequence's threads share one warp (the sub-transforms of Fft2L); each
+//               exchange is warp-synchronised: sync, write, sync, read.
+template <int N, bool INV, int SI, int NS, class AD = PadAddr, int STR = 1, class TWL = TwGlobal, bool WARP = false>
 struct FftStages {
   using P = FftPlan<N>;
   static __device__ __forceinline__ void run(float2 (&v)[P::E], float2* buf, int t,
-                                             const float2* __restrict__ tw) {
+                                             const float4* __restrict__ tw) {
     constexpr int E = P::E;
     constexpr int R = P::radix(INV, SI);
     constexpr int B = E / R;
@@ -117,26 +121,19 @@ struct FftStages {
 #pragma unroll
       for (int b = 0; b < B; ++b) {
         const int k = (t + b * T) % NS;
-#if RS_TW_STAGE_MAJOR
         constexpr int TW_OFF = (INV ? P::INV_BASE : 0) + P::stage_offset(INV, SI);
-        const float2* tws = tw + TW_OFF + k;
-#else
-        const int step = k * (N / (NS * R));
-#endif
+        const float4* tws = tw + TW_OFF + k;
 #pragma unroll
         for (int r = 1; r < R; ++r) {
-#if RS_TW_STAGE_MAJOR
-          const float2 w = TWL::load(&tws[(r - 1) * NS]);
-#else
-          const float2 w = TWL::load(&tw[r * step]);
-#endif
-          v[b * R + r] = INV ? cmulc(v[b * R + r], w) : cmul(v[b * R + r], w);
+          const float4 w = TWL::load(&tws[(r - 1) * NS]);
+          v[b * R + r] = INV ? cmulc_tw(v[b * R + r], w) : cmul_tw(v[b * R + r], w);
         }
       }
     }
     dft_all<R, INV, E>(v, std::make_integer_sequence<int, B>{});
     if constexpr (SI + 1 < P::NST) {
       constexpr int R2 = P::radix(INV, SI + 1);
+      if constexpr (WARP) __syncwarp();
 #pragma unroll
       for (int b = 0; b < B; ++b) {
         const int j = t + b * T;
@@ -144,22 +141,92 @@ struct FftStages {
 #pragma unroll
         for (int q = 0; q < R; ++q) buf[AD::at(base + q * NS) * STR] = v[b * R + q];
       }
-      __syncthreads();
+      if constexpr (WARP) __syncwarp(); else __syncthreads();
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = buf[AD::at(slot_pos<N, R2>(t, e)) * STR];
-      __syncthreads();
-      FftStages<N, INV, SI + 1, NS * R, AD, STR, TWL>::run(v, buf, t, tw);
+      if constexpr (!WARP) __syncthreads();
+      FftStages<N, INV, SI + 1, NS * R, AD, STR, TWL, WARP>::run(v, buf, t, tw);
     }
   }
 };
 
 // Full transform of one sequence. On entry v is in the entry mapping of this direction,
 // on exit in its exit mapping. Every thread of the block must call it (it synchronises).
-// tw: the stage-major tables (RS_TW_STAGE_MAJOR) or tw[m] = exp(-2*pi*i*m/N), m in [0, N).
+// tw: the stage-major tables of compensated twiddles (FftPlan::stage_offset).
 template <int N, bool INV, class AD = PadAddr, int STR = 1, class TWL = TwGlobal>
 __device__ __forceinline__ void fft_seq(float2 (&v)[FftPlan<N>::E], float2* buf, int t,
-                                        const float2* __restrict__ tw) {
+                                        const float4* __restrict__ tw) {
   FftStages<N, INV, 0, 1, AD, STR, TWL>::run(v, buf, t, tw);
+}
+
+// ------------------------------------------------------------------ two-level transform
+// For N = 16*T (power of two, T = N/16 threads per sequence, G = T/16 threads per group):
+//   X[c + 16 d] = sum_m W_T^{m d} [ W_N^{m c} sum_a x[m + T a] W_16^{a c} ]
+// Thread m computes the 16-point DFT over a of its entry values x[m + T a] and twiddles them by
+// W_N^{m c}; one block-wide exchange hands the T values of frequency c to the G threads
+// t = c*G + j; those G threads (one warp or part of one) run the T-point transform with
+// FftStages<T> and warp-level exchanges only. A transform therefore has a single block
+// barrier, against NST-1 pairs for the Stockham sequence.
+// Entry mapping (forward) : register e of thread t holds x[t + T e]      (as FftPlan<N>, radix 16)
+// Exit mapping  (forward) : register e of thread t holds X[exit_pos(t, e)]
+// The inverse runs the same steps backwards (exit mapping in, entry mapping out).
+// Block exchange: slot BX::at(c*T + m) holds frequency c of thread m; region c (slots of
+// c*T .. c*T+T-1) is read by group c only, and the group's own exchanges stay inside it (AD
+// addressing relative to the region base). With BX = NatAddr a thread's exchange slots are the
+// slots of its entry values, so a block that loaded its values from the buffer may overwrite
+// them without a barrier.
+// Twiddle table (compensated, float4): [0, 15T): W_N^{c m} at (c-1)*T + m; then FftPlan<T>'s
+// stage-major table.
+template <int N>
+struct Fft2L {
+  static constexpr int T = N / 16;
+  static constexpr int G = T / 16;
+  using SP = FftPlan<(T >= 16 ? T : 16)>;
+  static constexpr bool POW2 = (N & (N - 1)) == 0;
+  static constexpr int TW_LEN = 15 * T + SP::TW_USED;
+  // usable by a kernel that interleaves W sequences lane by lane (thread = t*W + column):
+  // the G*W threads of a group must form one aligned part of a warp
+  __host__ __device__ static constexpr bool ok(int W) { return POW2 && T >= 16 && G * W <= 32 && 32 % (G * W) == 0; }
+  static __device__ __forceinline__ int exit_pos(int t, int e) {
+    return t / G + 16 * slot_pos<T, SP::exit_radix(false)>(t % G, e);
+  }
+};
+
+template <int N, class BX, class AD, int STR, class TWL>
+__device__ __forceinline__ void fft2l_fwd(float2 (&v)[16], float2* buf, int t, const float4* __restrict__ tw) {
+  using F = Fft2L<N>;
+  constexpr int T = F::T;
+  constexpr int G = F::G;
+  dft16<false>(v);
+#pragma unroll
+  for (int c = 1; c < 16; ++c) v[c] = cmul_tw(v[c], TWL::load(&tw[(c - 1) * T + t]));
+#pragma unroll
+  for (int c = 0; c < 16; ++c) buf[BX::at(c * T + t) * STR] = v[c];
+  __syncthreads();
+  const int c = t / G;
+  const int j = t % G;
+#pragma unroll
+  for (int e = 0; e < 16; ++e) v[e] = buf[BX::at(c * T + j + e * G) * STR];
+  FftStages<T, false, 0, 1, AD, STR, TWL, true>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T);
+}
+
+template <int N, class BX, class AD, int STR, class TWL>
+__device__ __forceinline__ void fft2l_inv(float2 (&v)[16], float2* buf, int t, const float4* __restrict__ tw) {
+  using F = Fft2L<N>;
+  constexpr int T = F::T;
+  constexpr int G = F::G;
+  const int c = t / G;
+  const int j = t % G;
+  FftStages<T, true, 0, 1, AD, STR, TWL, true>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T);
+  __syncwarp();
+#pragma unroll
+  for (int e = 0; e < 16; ++e) buf[BX::at(c * T + j + e * G) * STR] = v[e];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < 16; ++k) v[k] = buf[BX::at(k * T + t) * STR];
+#pragma unroll
+  for (int k = 1; k < 16; ++k) v[k] = cmulc_tw(v[k], TWL::load(&tw[(k - 1) * T + t]));
+  dft16<true>(v);
 }
 
 }  // namespace rs

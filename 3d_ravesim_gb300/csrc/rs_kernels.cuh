@@ -38,6 +38,7 @@ struct AxisTab {
   const float* xf;
   const int* yi;
   const float* yf;
+  const int2* xp;      // x entries packed as {xi, bits of xf}: one 8-byte load per pixel
 };
 
 struct VoxelArgs {
@@ -47,14 +48,18 @@ struct VoxelArgs {
   const float2* db;    // (delta, beta) per material id; index 0 = vacuum
   int n_db;
   float a;             // thickness / wavelength
+  const float2* dbv;   // when set: (delta, beta) per voxel of this slice instead of ids + table
 };
 
 struct PlasmaArgs {
   const void* ne; const void* ni; const void* te; const void* zs;  // this z slice, (nyv, nxv)
   int f64;
   int nxv, nyv;
-  // delta = pref * (ne + ni*(1-q)*f1bar); beta = pref*ni*(1-q)*f2eff + cff*ne*ni*q^2/sqrt(te)
-  double pref, f1bar, f2eff, inv_zbar, zbar_pos, z2bar_pos, cff;
+  // With densities scaled by 1e-20: delta = pref20 * (ne + ni*(1-q)*f1bar);
+  // beta = pref20*ni*(1-q)*f2eff + cff*ne*ni*q^2/sqrt(te). All constants are rounded to float on
+  // the host, so the kernels carry no double-precision arithmetic for them.
+  float pref20, f1bar, f2eff, inv_zbar, cff;
+  int zbar_pos, z2bar_pos;
   float a;
 };
 
@@ -71,7 +76,7 @@ struct RowArgs {
   int ny;
   int flags;
   float scale;
-  const float2* tw;      // twiddles of length nx
+  const float4* tw;      // stage-major compensated twiddles of length nx
   AxisTab ax;
   VoxelArgs vox;
   PlasmaArgs pl;
@@ -85,10 +90,11 @@ struct ColArgs {
   int nx;
   int flags;
   float scale;
-  const float2* tw;      // twiddles of length ny
+  const float4* tw;      // stage-major compensated twiddles of length ny
   const float2* ex;      // nx entries: exp(-i pi wl dz kx^2)
   const float2* ey;      // ny entries: exp(2 pi i dz/wl) * exp(-i pi wl dz ky^2)
   const int* ylim;       // nx entries: largest |signed y index| kept by the cutoff, -1 = none
+  const float4* tw2;     // two-level twiddle table of length ny (Fft2L), when ny has one
 };
 
 // ----------------------------------------------------------------------------- physics
@@ -101,17 +107,29 @@ __device__ __forceinline__ float2 material_factor(float delta, float beta, float
   return make_float2(amp * c, -amp * s);
 }
 
-__device__ __forceinline__ float2 db_lookup(const VoxelArgs& p, const void* slice, int lin) {
+// (delta, beta) of one raw voxel id (the 32-bit word as stored in the grid).
+__device__ __forceinline__ float2 db_of_id(const VoxelArgs& p, uint32_t raw) {
   int id;
   if (p.grid_signed) {
-    id = static_cast<const int*>(slice)[lin];
+    id = static_cast<int>(raw);
     if (id < 0) id += p.n_db;  // numpy negative indexing of db_list
   } else {
-    const uint32_t u = static_cast<const uint32_t*>(slice)[lin];
-    id = u > 0x7fffffffu ? p.n_db : static_cast<int>(u);
+    id = raw > 0x7fffffffu ? p.n_db : static_cast<int>(raw);
   }
   id = min(max(id, 0), p.n_db - 1);  // ids are validated on the host; clamp keeps reads in bounds
   return __ldg(&p.db[id]);
+}
+
+__device__ __forceinline__ float2 db_lookup(const VoxelArgs& p, const void* slice, int lin) {
+  if (p.dbv) return __ldg(&p.dbv[lin]);
+  return db_of_id(p, static_cast<const uint32_t*>(slice)[lin]);
+}
+
+// a*(1-f) + b*f with the rounding spelled out (one product, one fused multiply-add), so that
+// every kernel that blends the same values gets the same bits whatever the compiler contracts.
+__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float f) {
+  const float g = __fsub_rn(1.0f, f);
+  return make_float2(__fmaf_rn(b.x, f, __fmul_rn(a.x, g)), __fmaf_rn(b.y, f, __fmul_rn(a.y, g)));
 }
 
 // Bilinear (delta, beta) at sim pixel with voxel corner (xi, yi) and fractions (fx, fy),
@@ -121,23 +139,13 @@ __device__ __forceinline__ float2 voxel_db(const VoxelArgs& p, int xi, float fx,
   const int l0 = yi * p.nxv + xi;
   const float2 d00 = db_lookup(p, p.slice, l0);
   float2 y0 = d00;
-  if (fx != 0.0f) {
-    const float2 d01 = db_lookup(p, p.slice, l0 + 1);
-    y0 = make_float2(d00.x * (1.0f - fx) + d01.x * fx, d00.y * (1.0f - fx) + d01.y * fx);
-  }
+  if (fx != 0.0f) y0 = lerp2(d00, db_lookup(p, p.slice, l0 + 1), fx);
   if (fy == 0.0f) return y0;
   const int l1 = l0 + p.nxv;
   const float2 d10 = db_lookup(p, p.slice, l1);
   float2 y1 = d10;
-  if (fx != 0.0f) {
-    const float2 d11 = db_lookup(p, p.slice, l1 + 1);
-    y1 = make_float2(d10.x * (1.0f - fx) + d11.x * fx, d10.y * (1.0f - fx) + d11.y * fx);
-  }
-  return make_float2(y0.x * (1.0f - fy) + y1.x * fy, y0.y * (1.0f - fy) + y1.y * fy);
-}
-
-__device__ __forceinline__ float2 lerp2(float2 a, float2 b, float f) {
-  return make_float2(a.x * (1.0f - f) + b.x * f, a.y * (1.0f - f) + b.y * f);
+  if (fx != 0.0f) y1 = lerp2(d10, db_lookup(p, p.slice, l1 + 1), fx);
+  return lerp2(y0, y1, fy);
 }
 
 // Voxel column j of grid row yi blended in y with weight fy (zero-weight rows are not read).
@@ -147,33 +155,113 @@ __device__ __forceinline__ float2 voxel_col_blend(const VoxelArgs& p, int j, int
   return lerp2(d0, db_lookup(p, p.slice, (yi + 1) * p.nxv + j), fy);
 }
 
-__device__ __forceinline__ double plasma_load(const void* g, int f64, int lin) {
-  return f64 ? __ldg(static_cast<const double*>(g) + lin)
-             : static_cast<double>(__ldg(static_cast<const float*>(g) + lin));
+// A grid value as float (float64 grids are rounded once; 1e21-scale densities fit in float).
+__device__ __forceinline__ float plasma_load(const void* g, int f64, int lin) {
+  return f64 ? __double2float_rn(__ldg(static_cast<const double*>(g) + lin))
+             : __ldg(static_cast<const float*>(g) + lin);
 }
 
 // delta, beta of one plasma voxel (big-wave/plasma.py:380-434), FP32 arithmetic on
-// pre-scaled densities so that n_e*n_i (~1e42 cm^-6) never overflows.
-__device__ __forceinline__ float2 plasma_db_voxel(const PlasmaArgs& p, int lin) {
-  const float ne = static_cast<float>(plasma_load(p.ne, p.f64, lin) * 1e-20);
-  const float ni = static_cast<float>(plasma_load(p.ni, p.f64, lin) * 1e-20);
-  const float te = static_cast<float>(plasma_load(p.te, p.f64, lin));
-  const float zs = static_cast<float>(plasma_load(p.zs, p.f64, lin));
-  float q = p.zbar_pos ? zs * static_cast<float>(p.inv_zbar) : 0.0f;
+// pre-scaled densities (ne, ni times 1e-20) so that n_e*n_i (~1e42 cm^-6) never overflows.
+__device__ __forceinline__ float2 plasma_db_vals(const PlasmaArgs& p, float ne, float ni, float te, float zs) {
+  float q = p.zbar_pos ? zs * p.inv_zbar : 0.0f;
   q = fminf(fmaxf(q, 0.0f), 1.0f);
   const float fb = 1.0f - q;
-  const float pref = static_cast<float>(p.pref * 1e20);
-  float delta = ne * pref;
+  float delta = ne * p.pref20;
   float beta = 0.0f;
   if (fb > 0.0f && ni > 0.0f) {
-    const float bs = ni * pref * fb;
-    delta += bs * static_cast<float>(p.f1bar);
-    beta += bs * static_cast<float>(p.f2eff);
+    const float bs = ni * p.pref20 * fb;
+    delta += bs * p.f1bar;
+    beta += bs * p.f2eff;
   }
   if (ne > 0.0f && ni > 0.0f && q > 0.0f && p.z2bar_pos && te > 0.0f) {
-    beta += static_cast<float>(p.cff) * ne * ni * q * q * rsqrtf(te);
+    beta += p.cff * ne * ni * q * q * rsqrtf(te);
   }
   return make_float2(delta, beta);
+}
+
+__device__ __forceinline__ float2 plasma_db_voxel(const PlasmaArgs& p, int lin) {
+  return plasma_db_vals(p, plasma_load(p.ne, p.f64, lin) * 1e-20f, plasma_load(p.ni, p.f64, lin) * 1e-20f,
+                        plasma_load(p.te, p.f64, lin), plasma_load(p.zs, p.f64, lin));
+}
+
+// ------------------------------------------------------------- voxel-row prefetch
+// The row pass copies the two voxel rows (yi, yi + 1) its transmission needs into shared memory
+// with asynchronous 4-byte copies issued before the inverse row transform, so the gathers'
+// latency hides behind that transform. The rows are contiguous in every grid, so each source
+// is one range of 2 * nxv elements.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// 4-byte words of one source's two rows: ids (4 B), per-voxel (delta, beta) (8 B), plasma
+// fields (4 or 8 B each, four sources).
+__device__ __forceinline__ int prefetch_words(bool vox, const VoxelArgs& v, const PlasmaArgs& pl) {
+  const int nxv = vox ? v.nxv : pl.nxv;
+  if (vox) return 2 * nxv * (v.dbv ? 2 : 1);
+  return 4 * 2 * nxv * (pl.f64 ? 2 : 1);
+}
+
+// Issue the copies of rows yi, yi + 1 into pf (uint32 words); src order: ids or dbv, or the
+// plasma fields ne, ni, te, zs one after the other.
+__device__ __forceinline__ void prefetch_rows(uint32_t* pf, bool vox, const VoxelArgs& v, const PlasmaArgs& pl,
+                                              int yi, int t, int nthreads) {
+  if (vox) {
+    const int w = v.dbv ? 2 : 1;
+    const int words = 2 * v.nxv * w;
+    const uint32_t* src = v.dbv ? reinterpret_cast<const uint32_t*>(v.dbv) + static_cast<size_t>(yi) * v.nxv * 2
+                                : static_cast<const uint32_t*>(v.slice) + static_cast<size_t>(yi) * v.nxv;
+    for (int i = t; i < words; i += nthreads) cp_async4(pf + i, src + i);
+  } else {
+    const int w = pl.f64 ? 2 : 1;
+    const int words = 2 * pl.nxv * w;
+    const void* f[4] = {pl.ne, pl.ni, pl.te, pl.zs};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t* src = static_cast<const uint32_t*>(f[k]) + static_cast<size_t>(yi) * pl.nxv * w;
+      for (int i = t; i < words; i += nthreads) cp_async4(pf + k * words + i, src + i);
+    }
+  }
+}
+
+__device__ __forceinline__ float pf_plasma(const uint32_t* pf, int f64, int idx) {
+  return f64 ? __double2float_rn(reinterpret_cast<const double*>(pf)[idx]) : __uint_as_float(pf[idx]);
+}
+
+// Voxel column j of the prefetched rows blended in y with weight fy.
+__device__ __forceinline__ float2 pf_col_blend(const uint32_t* pf, bool vox, const VoxelArgs& v,
+                                               const PlasmaArgs& pl, int j, float fy) {
+  if (vox) {
+    const int nxv = v.nxv;
+    float2 d0, d1;
+    if (v.dbv) {
+      const float2* r = reinterpret_cast<const float2*>(pf);
+      d0 = r[j];
+      if (fy == 0.0f) return d0;
+      d1 = r[nxv + j];
+    } else {
+      d0 = db_of_id(v, pf[j]);
+      if (fy == 0.0f) return d0;
+      d1 = db_of_id(v, pf[nxv + j]);
+    }
+    return lerp2(d0, d1, fy);
+  }
+  const int nxv = pl.nxv;
+  const int words = 2 * nxv * (pl.f64 ? 2 : 1);
+  const uint32_t* ne = pf;
+  const uint32_t* ni = pf + words;
+  const uint32_t* te = pf + 2 * words;
+  const uint32_t* zs = pf + 3 * words;
+  auto at = [&](int k) {
+    return plasma_db_vals(pl, pf_plasma(ne, pl.f64, k) * 1e-20f, pf_plasma(ni, pl.f64, k) * 1e-20f,
+                          pf_plasma(te, pl.f64, k), pf_plasma(zs, pl.f64, k));
+  };
+  const float2 d0 = at(j);
+  if (fy == 0.0f) return d0;
+  return lerp2(d0, at(nxv + j), fy);
 }
 
 __device__ __forceinline__ float2 plasma_db(const PlasmaArgs& p, int xi, float fx, int yi, float fy) {
@@ -182,9 +270,7 @@ __device__ __forceinline__ float2 plasma_db(const PlasmaArgs& p, int xi, float f
   const float2 d01 = plasma_db_voxel(p, l0 + 1);
   const float2 d10 = plasma_db_voxel(p, l0 + p.nxv);
   const float2 d11 = plasma_db_voxel(p, l0 + p.nxv + 1);
-  const float2 y0 = make_float2(d00.x * (1.0f - fx) + d01.x * fx, d00.y * (1.0f - fx) + d01.y * fx);
-  const float2 y1 = make_float2(d10.x * (1.0f - fx) + d11.x * fx, d10.y * (1.0f - fx) + d11.y * fx);
-  return make_float2(y0.x * (1.0f - fy) + y1.x * fy, y0.y * (1.0f - fy) + y1.y * fy);
+  return lerp2(lerp2(d00, d01, fx), lerp2(d10, d11, fx), fy);
 }
 
 __device__ __forceinline__ float2 plasma_col_blend(const PlasmaArgs& p, int j, int yi, float fy) {
@@ -243,6 +329,18 @@ constexpr int row_minb() {
   return ROWS * FftPlan<N>::T <= 256 ? (FftPlan<N>::E == 16 ? RS_ROW_MINB : 2) : 1;
 }
 
+// Shared memory of a row block: the exchange buffers (S per row), then a voxel-row prefetch
+// area of PF_WORDS 4-byte words per row (at most 8 KB: two rows of up to 1024 ids; larger rows
+// are gathered without it). It is kept small so that L1 keeps room for the twiddle tables, and
+// PF_WORDS <= 2*S, so whatever fits it also fits the staging buffer.
+template <int N, int ROWS>
+struct RowGeom {
+  static constexpr size_t BUF = static_cast<size_t>(ROWS) * FftPlan<N>::S * sizeof(float2);
+  static constexpr int PF_WORDS = 2 * FftPlan<N>::S < 2048 ? 2 * FftPlan<N>::S : 2048;
+  static constexpr bool PF = BUF + static_cast<size_t>(ROWS) * PF_WORDS * 4 <= 200 * 1024;
+  static constexpr size_t SMEM = PF ? BUF + static_cast<size_t>(ROWS) * PF_WORDS * 4 : BUF;
+};
+
 template <int N, int ROWS>
 __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row_pass_kernel(const RowArgs a) {
   using P = FftPlan<N>;
@@ -260,6 +358,24 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   constexpr int E = P::E;
   float2 v[E];
 
+  // Transmission row coordinates, and the prefetch of its two voxel rows (block-uniform decision).
+  const bool tmode = flags & (ROW_TVOX | ROW_TPLASMA);
+  const bool vox = flags & ROW_TVOX;
+  int yi = -1;
+  float fy = 0.0f;
+  bool pf_on = false;
+  uint32_t* pf = reinterpret_cast<uint32_t*>(smem + ROWS * P::S) + lr * RowGeom<N, ROWS>::PF_WORDS;
+  if (tmode) {
+    if (valid) {
+      yi = __ldg(&a.ax.yi[row]);
+      if (yi >= 0) fy = __ldg(&a.ax.yf[row]);
+    }
+    if constexpr (RowGeom<N, ROWS>::PF) {
+      pf_on = prefetch_words(vox, a.vox, a.pl) <= RowGeom<N, ROWS>::PF_WORDS;
+      if (pf_on && yi >= 0) prefetch_rows(pf, vox, a.vox, a.pl, yi, t, T);
+    }
+  }
+
   if (flags & ROW_INV) {
 #pragma unroll
     for (int e = 0; e < E; ++e)
@@ -274,19 +390,19 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
       v[e] = valid ? a.in[rbase + slot_pos<N, RF>(t, e)] : make_float2(0.f, 0.f);
   }
 
-  if (flags & (ROW_TVOX | ROW_TPLASMA)) {
+  if (tmode) {
     // The exchange buffer is idle between the two transforms: stage the voxel row blended in y
     // there (one gather per voxel column instead of four per pixel), then interpolate in x.
-    const bool vox = flags & ROW_TVOX;
     const int nxv = vox ? a.vox.nxv : a.pl.nxv;
     const bool staged = nxv <= P::S;  // uniform across the block
-    int yi = -1;
-    float fy = 0.0f;
-    if (valid) {
-      yi = __ldg(&a.ax.yi[row]);
-      if (yi >= 0) fy = __ldg(&a.ax.yf[row]);
-    }
-    if (staged) {
+    if (pf_on) {
+      cp_async_wait_all();
+      __syncthreads();
+      if (yi >= 0) {
+        for (int j = t; j < nxv; j += T) buf[j] = pf_col_blend(pf, vox, a.vox, a.pl, j, fy);
+      }
+      __syncthreads();
+    } else if (staged) {
       if (yi >= 0) {
         for (int j = t; j < nxv; j += T) buf[j] = vox ? voxel_col_blend(a.vox, j, yi, fy) : plasma_col_blend(a.pl, j, yi, fy);
       }
@@ -304,9 +420,10 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
       for (int i = 0; i < CH; ++i) {
         d[i] = make_float2(0.f, 0.f);
         const int x = slot_pos<N, RF>(t, c0 + i);
-        const int xi = yi >= 0 ? __ldg(&a.ax.xi[x]) : -1;
+        const int2 xe = yi >= 0 ? __ldg(&a.ax.xp[x]) : make_int2(-1, 0);
+        const int xi = xe.x;
         if (xi >= 0) {
-          const float fx = __ldg(&a.ax.xf[x]);
+          const float fx = __int_as_float(xe.y);
           if (staged) {
             d[i] = buf[xi];
             if (fx != 0.0f) d[i] = lerp2(d[i], buf[xi + 1], fx);
@@ -353,11 +470,18 @@ struct ColGeom {
   static constexpr size_t SMEM = static_cast<size_t>(W) * SC * sizeof(float2);
 };
 
+// Column position held by register e of thread t after the forward column transform.
+template <int N, bool L2>
+__device__ __forceinline__ int col_exit_pos(int t, int e) {
+  if constexpr (L2) return Fft2L<N>::exit_pos(t, e);
+  else return slot_pos<N, FftPlan<N>::exit_radix(false)>(t, e);
+}
+
 template <int N, int W>
 __global__ void __launch_bounds__(W * FftPlan<N>::T) col_pass_kernel(const ColArgs a) {
   using P = FftPlan<N>;
+  constexpr bool L2 = Fft2L<N>::ok(W);  // two-level column transforms (one block barrier each)
   constexpr int RF = P::entry_radix(false);
-  constexpr int RX = P::exit_radix(false);
   extern __shared__ float2 smem[];
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
@@ -373,10 +497,11 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T) col_pass_kernel(const ColAr
   if (flags & COL_FWD) {
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = a.in[static_cast<size_t>(slot_pos<N, RF>(t, e)) * nx + x];
-    fft_seq<N, false>(v, buf, t, a.tw);
+    if constexpr (L2) fft2l_fwd<N, PadAddr, PadAddr, 1, TwGlobal>(v, buf, t, a.tw2);
+    else fft_seq<N, false>(v, buf, t, a.tw);
   } else {
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = a.in[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x];
+    for (int e = 0; e < E; ++e) v[e] = a.in[static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * nx + x];
   }
 
   // registers are in the forward-exit (== inverse-entry) mapping: position = fy
@@ -385,7 +510,7 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T) col_pass_kernel(const ColAr
     const float2 exv = (flags & COL_H) ? __ldg(&a.ex[x]) : make_float2(1.f, 0.f);
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const int fy = slot_pos<N, RX>(t, e);
+      const int fy = col_exit_pos<N, L2>(t, e);
       const int m = fy < (N + 1) / 2 ? fy : fy - N;
       const bool keep = (m < 0 ? -m : m) <= lim;
       if (!keep) {
@@ -397,21 +522,22 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T) col_pass_kernel(const ColAr
   }
   if ((flags & COL_SPEC) && live) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x] = v[e];
+    for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * nx + x] = v[e];
   }
   if (flags & COL_SCALE) {
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = cscale(v[e], a.scale);
   }
   if (flags & COL_INV) {
-    fft_seq<N, true>(v, buf, t, a.tw);
+    if constexpr (L2) fft2l_inv<N, PadAddr, PadAddr, 1, TwGlobal>(v, buf, t, a.tw2);
+    else fft_seq<N, true>(v, buf, t, a.tw);
     if (live) {
 #pragma unroll
       for (int e = 0; e < E; ++e) a.out[static_cast<size_t>(slot_pos<N, RF>(t, e)) * nx + x] = v[e];
     }
   } else if (live) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) a.out[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x] = v[e];
+    for (int e = 0; e < E; ++e) a.out[static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * nx + x] = v[e];
   }
 }
 
@@ -421,10 +547,12 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T) col_pass_kernel(const ColAr
 void note_launch(unsigned n = 1);
 
 cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s);
-// Twiddles used by the fused passes of length n (fast sizes only): stage-major tables, or the
-// plain table tw[m] = exp(-2*pi*i*m/n) when RS_TW_STAGE_MAJOR is 0.
-cudaError_t launch_stage_twiddles(int n, float2* tw, cudaStream_t s);
+// Compensated stage-major twiddle tables of the fused passes for length n (fast sizes only).
+cudaError_t launch_stage_twiddles(int n, float4* tw, cudaStream_t s);
 int stage_twiddle_len(int n);
+// Two-level column-transform table of length n (0 when n has none) and its builder.
+int twiddles_2l_len(int n);
+cudaError_t launch_twiddles_2l(int n, float4* tw, cudaStream_t s);
 cudaError_t launch_col_pass(int ny, const ColArgs& a, cudaStream_t s);
 bool fast_size(int n);
 

@@ -80,8 +80,11 @@ __global__ void axis_table_kernel(const AxisTabArgs a) {
   const double idx = __ddiv_rn(__dadd_rn(__dadd_rn(__dmul_rn(sim, a.cs), a.pos), half), a.pitch);
   const double fl = floor(idx);
   const bool inside = (idx >= 0.0) && (idx < static_cast<double>(a.len) - 1.0);
-  a.idx[i] = inside ? static_cast<int>(fl) : -1;
-  a.frac[i] = static_cast<float>(__dsub_rn(idx, fl));
+  const int id = inside ? static_cast<int>(fl) : -1;
+  const float fr = static_cast<float>(__dsub_rn(idx, fl));
+  a.idx[i] = id;
+  a.frac[i] = fr;
+  if (a.packed) a.packed[i] = make_int2(id, __float_as_int(fr));
 }
 
 // One block per line; the line is staged in shared memory, so in == out is allowed.
@@ -177,7 +180,93 @@ __global__ void detector_kernel(const DetArgs a) {
   a.out[o] = a.accumulate ? a.out[o] + val : val;
 }
 
+// One block per field row. The row's voxel rows (yi, yi+1) get their gradient contributions
+// summed in shared memory first (shared atomics), then one global atomic per touched entry.
+__global__ void adjoint_slice_kernel(const AdjointSliceArgs a) {
+  extern __shared__ float acc[];  // 4 * nxv floats: (d, b) of voxel rows yi and yi + 1
+  const int y = blockIdx.x;
+  const int nxv = a.nxv;
+  for (int j = threadIdx.x; j < 4 * nxv; j += blockDim.x) acc[j] = 0.0f;
+  __syncthreads();
+  const int yi = __ldg(&a.ax.yi[y]);
+  const float fy = yi >= 0 ? __ldg(&a.ax.yf[y]) : 0.0f;
+  const size_t rb = static_cast<size_t>(y) * a.nx;
+  for (int x = threadIdx.x; x < a.nx; x += blockDim.x) {
+    const int xi = __ldg(&a.ax.xi[x]);
+    const float2 vv = a.v[rb + x];
+    if (yi < 0 || xi < 0) continue;  // outside the grid: t = 1, no voxel depends on this pixel
+    const float fx = __ldg(&a.ax.xf[x]);
+    const float2* r0 = a.dbv + static_cast<size_t>(yi) * nxv;
+    const float2* r1 = r0 + nxv;
+    const float2 d0 = lerp2(__ldg(&r0[xi]), __ldg(&r0[xi + 1]), fx);
+    const float2 d1 = lerp2(__ldg(&r1[xi]), __ldg(&r1[xi + 1]), fx);
+    const float2 d = lerp2(d0, d1, fy);
+    const float2 t = material_factor(d.x, d.y, a.a);
+    const float2 uu = __ldg(&a.u[rb + x]);
+    // G = conj(u) v; q = conj(G) t; dL/ddelta = 4 pi a Im(q); dL/dbeta = -4 pi a Re(q)
+    const float2 G = make_float2(fmaf(uu.x, vv.x, uu.y * vv.y), fmaf(uu.x, vv.y, -uu.y * vv.x));
+    const float2 q = cmulc(t, G);
+    const float k = 12.566370614359172f * a.a;
+    const float gd = k * q.y, gb = -k * q.x;
+    const float w00 = (1.0f - fx) * (1.0f - fy), w01 = fx * (1.0f - fy), w10 = (1.0f - fx) * fy, w11 = fx * fy;
+    atomicAdd(&acc[2 * xi], w00 * gd);
+    atomicAdd(&acc[2 * xi + 1], w00 * gb);
+    atomicAdd(&acc[2 * xi + 2], w01 * gd);
+    atomicAdd(&acc[2 * xi + 3], w01 * gb);
+    atomicAdd(&acc[2 * nxv + 2 * xi], w10 * gd);
+    atomicAdd(&acc[2 * nxv + 2 * xi + 1], w10 * gb);
+    atomicAdd(&acc[2 * nxv + 2 * xi + 2], w11 * gd);
+    atomicAdd(&acc[2 * nxv + 2 * xi + 3], w11 * gb);
+    a.v[rb + x] = cmulc(vv, t);  // conj(t) * v
+  }
+  __syncthreads();
+  if (yi < 0) return;
+  float* g0 = reinterpret_cast<float*>(a.grad + static_cast<size_t>(yi) * nxv);
+  for (int j = threadIdx.x; j < 4 * nxv; j += blockDim.x) {
+    const float val = acc[j];
+    if (val != 0.0f) atomicAdd(&g0[j], val);  // rows yi and yi + 1 are contiguous in the grid
+  }
+}
+
+__global__ void detector_adjoint_kernel(const DetAdjArgs a) {
+  const int gx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gy = blockIdx.y;
+  if (gx >= a.nx || gy >= a.ny) return;
+  double sacc = 0.0;
+  const int y0 = __ldg(&a.yptr[gy]), y1 = __ldg(&a.yptr[gy + 1]);
+  const int x0 = __ldg(&a.xptr[gx]), x1 = __ldg(&a.xptr[gx + 1]);
+  for (int yk = y0; yk < y1; ++yk) {
+    const int oy = __ldg(&a.ydet[yk]);
+    const double yd = __ldg(&a.ypos[oy]);
+    double inner = 0.0;
+    for (int xk = x0; xk < x1; ++xk) {
+      const int ox = __ldg(&a.xdet[xk]);
+      const double xd = __ldg(&a.xpos[ox]);
+      const double cosine = a.z / sqrt(xd * xd + yd * yd + a.z * a.z);
+      inner += static_cast<double>(__ldg(&a.xw[xk])) * cosine * a.r[static_cast<size_t>(oy) * a.out_x + ox];
+    }
+    sacc += __ldg(&a.yw[yk]) * inner;
+  }
+  const size_t i = static_cast<size_t>(gy) * a.nx + gx;
+  a.g[i] = cscale(a.u[i], static_cast<float>(sacc));
+}
+
 }  // namespace
+
+cudaError_t launch_adjoint_slice(const AdjointSliceArgs& a, cudaStream_t s) {
+  const size_t smem = static_cast<size_t>(4) * a.nxv * sizeof(float);
+  if (smem > 200 * 1024) return cudaErrorInvalidValue;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(adjoint_slice_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  adjoint_slice_kernel<<<a.ny, 256, smem, s>>>(a);
+  return counted(cudaGetLastError());
+}
+
+cudaError_t launch_detector_adjoint(const DetAdjArgs& a, cudaStream_t s) {
+  dim3 grid((a.nx + 127) / 128, a.ny);
+  detector_adjoint_kernel<<<grid, 128, 0, s>>>(a);
+  return counted(cudaGetLastError());
+}
 
 cudaError_t launch_twiddles(float2* tw, int n, cudaStream_t s) {
   twiddle_kernel<<<nblocks(n), kTPB, 0, s>>>(tw, n);

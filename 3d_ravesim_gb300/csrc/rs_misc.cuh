@@ -27,6 +27,7 @@ struct AxisTabArgs {
   double pitch;     // voxel pitch
   int* idx;
   float* frac;
+  int2* packed;     // optional {idx, bits of frac} copy
 };
 
 struct DetArgs {
@@ -53,5 +54,33 @@ cudaError_t launch_point_source(float2* u, int nx, int ny, const PointSrcArgs& p
 cudaError_t launch_transmission(float2* u, int nx, int ny, const AxisTab& ax, const VoxelArgs* vox,
                                 const PlasmaArgs* pl, cudaStream_t s);
 cudaError_t launch_detector(const DetArgs& a, cudaStream_t s);
+
+// Adjoint of one slice of the multislice forward u' = P (t * u): given v = P^H g' (in `v`),
+// accumulates dL/d(delta, beta) of the slice's voxels (float2 per voxel, `grad`) through the
+// bilinear weights and replaces v by conj(t) * v = dL/dconj(u).
+struct AdjointSliceArgs {
+  float2* v;
+  const float2* u;          // forward field entering the slice (before its transmission)
+  const float2* dbv;        // (delta, beta) per voxel of this slice, (nyv, nxv)
+  float2* grad;             // dL/d(delta, beta) per voxel of this slice
+  int nx, ny, nxv, nyv;
+  AxisTab ax;
+  float a;                  // thickness / wavelength
+};
+cudaError_t launch_adjoint_slice(const AdjointSliceArgs& a, cudaStream_t s);
+
+// Transposed detector: g = s * u with s(cell) = sum over overlapping detector pixels of
+// weight * cosine * r(pixel) (inverse overlap tables per axis, built on the host).
+struct DetAdjArgs {
+  const float2* u;
+  float2* g;
+  const double* r;          // dL/dI, (out_y, out_x)
+  int nx, ny, out_x;
+  const int* xptr; const int* xdet; const float* xw;      // per grid column: detector columns
+  const int* yptr; const int* ydet; const double* yw;     // per grid row: detector rows
+  const double* xpos; const double* ypos;                  // detector pixel centres
+  double z;
+};
+cudaError_t launch_detector_adjoint(const DetAdjArgs& a, cudaStream_t s);
 
 }  // namespace rs

@@ -26,10 +26,29 @@ cudaError_t launch_col_pass_pow2(int n, const ColArgs& a, cudaStream_t s) {
   }
 }
 
-cudaError_t launch_stage_twiddles_pow2(int n, float2* tw, cudaStream_t s) {
+cudaError_t launch_stage_twiddles_pow2(int n, float4* tw, cudaStream_t s) {
   switch (n) {
     RS_POW2_SIZES(RS_TW_CASE)
     default: return cudaErrorInvalidValue;
+  }
+}
+
+#define RS_TW2L_CASE(N) \
+  case N: return launch_twiddles_2l_n<N>(tw, s);
+#define RS_TW2LLEN_CASE(N) \
+  case N: return (Fft2L<N>::POW2 && Fft2L<N>::T >= 16) ? Fft2L<N>::TW_LEN : 0;
+
+cudaError_t launch_twiddles_2l_pow2(int n, float4* tw, cudaStream_t s) {
+  switch (n) {
+    RS_POW2_SIZES(RS_TW2L_CASE)
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+int twiddles_2l_len_pow2(int n) {
+  switch (n) {
+    RS_POW2_SIZES(RS_TW2LLEN_CASE)
+    default: return 0;
   }
 }
 

@@ -26,7 +26,7 @@ cudaError_t launch_col_pass_pow3(int n, const ColArgs& a, cudaStream_t s) {
   }
 }
 
-cudaError_t launch_stage_twiddles_pow3(int n, float2* tw, cudaStream_t s) {
+cudaError_t launch_stage_twiddles_pow3(int n, float4* tw, cudaStream_t s) {
   switch (n) {
     RS_POW3_SIZES(RS_TW_CASE)
     default: return cudaErrorInvalidValue;

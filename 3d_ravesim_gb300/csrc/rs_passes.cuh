@@ -16,7 +16,7 @@ template <int N>
 cudaError_t launch_rows_n(const RowArgs& a, cudaStream_t s) {
   constexpr int ROWS = rows_per_block<N>();
   constexpr int THREADS = ROWS * FftPlan<N>::T;
-  constexpr size_t SMEM = static_cast<size_t>(ROWS) * FftPlan<N>::S * sizeof(float2);
+  constexpr size_t SMEM = RowGeom<N, ROWS>::SMEM;
   static unsigned configured = 0;  // one bit per device ordinal
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
@@ -35,14 +35,20 @@ cudaError_t launch_rows_n(const RowArgs& a, cudaStream_t s) {
   return e;
 }
 
-// Stage-major twiddle tables (forward plan, then inverse plan) in FP64, rounded to float.
+// exp(-2*pi*i*m/N) evaluated in FP64, split into a float and the float of its residual.
+__device__ __forceinline__ float4 twiddle_fp64(long long m, int n) {
+  double sn, cs;
+  sincospi(-2.0 * static_cast<double>(m) / static_cast<double>(n), &sn, &cs);
+  const float ch = static_cast<float>(cs), sh = static_cast<float>(sn);
+  return make_float4(ch, sh, static_cast<float>(cs - static_cast<double>(ch)),
+                     static_cast<float>(sn - static_cast<double>(sh)));
+}
+
+// Entry i of FftPlan<N>'s stage-major tables (forward plan, then inverse plan).
 template <int N>
-__global__ void stage_twiddles_kernel(float2* tw) {
+__device__ __forceinline__ float4 stage_twiddle(int i) {
   using P = FftPlan<N>;
   constexpr int NF = P::table_len(false);
-  constexpr int NI = P::table_len(true);
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= NF + NI) return;
   const bool inv = i >= NF;
   const int j = inv ? i - NF : i;
   int s = 1;
@@ -50,14 +56,42 @@ __global__ void stage_twiddles_kernel(float2* tw) {
   const int ns = P::ns(inv, s);
   const int r = (j - P::stage_offset(inv, s)) / ns + 1;
   const int k = (j - P::stage_offset(inv, s)) % ns;
-  const long long m = static_cast<long long>(r) * k * (N / (ns * P::radix(inv, s)));
-  double sn, cs;
-  sincospi(-2.0 * static_cast<double>(m) / static_cast<double>(N), &sn, &cs);
-  tw[i] = make_float2(static_cast<float>(cs), static_cast<float>(sn));
+  return twiddle_fp64(static_cast<long long>(r) * k * (N / (ns * P::radix(inv, s))), N);
 }
 
 template <int N>
-cudaError_t launch_stage_twiddles_n(float2* tw, cudaStream_t s) {
+__global__ void stage_twiddles_kernel(float4* tw) {
+  using P = FftPlan<N>;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= P::table_len(false) + P::table_len(true)) return;
+  tw[i] = stage_twiddle<N>(i);
+}
+
+// Two-level table (Fft2L<N>): W_N^{c m} at (c-1)*T + m, then FftPlan<T>'s stage-major table.
+template <int N>
+__global__ void twiddles_2l_kernel(float4* tw) {
+  using F = Fft2L<N>;
+  constexpr int T = F::T;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= F::TW_LEN) return;
+  if (i < 15 * T) tw[i] = twiddle_fp64(static_cast<long long>(i / T + 1) * (i % T), N);
+  else tw[i] = stage_twiddle<T>(i - 15 * T);
+}
+
+template <int N>
+cudaError_t launch_twiddles_2l_n(float4* tw, cudaStream_t s) {
+  if constexpr (!Fft2L<N>::POW2 || Fft2L<N>::T < 16) {
+    return cudaErrorInvalidValue;
+  } else {
+    twiddles_2l_kernel<N><<<(Fft2L<N>::TW_LEN + 255) / 256, 256, 0, s>>>(tw);
+    const cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) note_launch();
+    return e;
+  }
+}
+
+template <int N>
+cudaError_t launch_stage_twiddles_n(float4* tw, cudaStream_t s) {
   constexpr int total = FftPlan<N>::table_len(false) + FftPlan<N>::table_len(true);
   if (total == 0) return cudaSuccess;
   stage_twiddles_kernel<N><<<(total + 255) / 256, 256, 0, s>>>(tw);
@@ -186,8 +220,11 @@ cudaError_t launch_row_pass_pow2(int n, const RowArgs& a, cudaStream_t s);
 cudaError_t launch_row_pass_pow3(int n, const RowArgs& a, cudaStream_t s);
 cudaError_t launch_col_pass_pow2(int n, const ColArgs& a, cudaStream_t s);
 cudaError_t launch_col_pass_pow3(int n, const ColArgs& a, cudaStream_t s);
-cudaError_t launch_stage_twiddles_pow2(int n, float2* tw, cudaStream_t s);
-cudaError_t launch_stage_twiddles_pow3(int n, float2* tw, cudaStream_t s);
+cudaError_t launch_stage_twiddles_pow2(int n, float4* tw, cudaStream_t s);
+// Two-level column-transform table (power-of-two n >= 256); length 0 when n has none.
+int twiddles_2l_len_pow2(int n);
+cudaError_t launch_twiddles_2l_pow2(int n, float4* tw, cudaStream_t s);
+cudaError_t launch_stage_twiddles_pow3(int n, float4* tw, cudaStream_t s);
 int stage_twiddle_len_pow2(int n);
 int stage_twiddle_len_pow3(int n);
 

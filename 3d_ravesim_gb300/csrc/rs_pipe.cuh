@@ -112,14 +112,15 @@ struct ColPipeGeom {
   static constexpr int NB = (3 * TILE * 8 <= 200 * 1024) ? 3 : 2;
   static constexpr int THREADS = W * T;
   // twiddles (forward and inverse stage-major tables) copied to shared memory when they fit
-  static constexpr int TW_LEN = FftPlan<N>::TW_USED;
+  static constexpr bool L2 = Fft2L<N>::ok(W);                 // two-level column transforms
+  static constexpr int TW_LEN = L2 ? Fft2L<N>::TW_LEN : FftPlan<N>::TW_USED;
   static constexpr size_t TILES_BYTES = static_cast<size_t>(NB) * TILE * sizeof(float2);
-  static constexpr size_t TW_BYTES = static_cast<size_t>((TW_LEN + 1) / 2 * 2) * sizeof(float2);
+  static constexpr size_t TW_BYTES = static_cast<size_t>(TW_LEN) * sizeof(float4);
 #ifndef RS_COLPIPE_TW_SMEM
 #define RS_COLPIPE_TW_SMEM 1
 #endif
   static constexpr bool TW_SMEM =
-      RS_COLPIPE_TW_SMEM && RS_TW_STAGE_MAJOR && TW_LEN > 0 && TILES_BYTES + TW_BYTES + 64 <= 227 * 1024;
+      RS_COLPIPE_TW_SMEM && TW_LEN > 0 && TILES_BYTES + TW_BYTES + 64 <= 227 * 1024;
   static constexpr size_t SMEM = TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + NB * sizeof(uint64_t);
 };
 
@@ -271,11 +272,10 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
   constexpr int W = G::W;
   constexpr int E = P::E;
   constexpr int RF = P::entry_radix(false);
-  constexpr int RX = P::exit_radix(false);
   constexpr uint32_t TILE_BYTES = G::TILE * 8u;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   float2* tiles = reinterpret_cast<float2*>(smem_raw);
-  float2* tw_s = tiles + G::NB * G::TILE;
+  float4* tw_s = reinterpret_cast<float4*>(tiles + G::NB * G::TILE);
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + G::TILES_BYTES + (G::TW_SMEM ? G::TW_BYTES : 0));
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
@@ -288,11 +288,12 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
   }
   __syncthreads();
 
+  const float4* tw_g = G::L2 ? a.tw2 : a.tw;
   if constexpr (G::TW_SMEM) {  // the block's copy of the twiddle tables (read from L2 once)
-    for (int i = threadIdx.x; i < G::TW_LEN; i += blockDim.x) tw_s[i] = __ldg(&a.tw[i]);
+    for (int i = threadIdx.x; i < G::TW_LEN; i += blockDim.x) tw_s[i] = __ldg(&tw_g[i]);
     __syncthreads();
   }
-  const float2* tw = G::TW_SMEM ? tw_s : a.tw;
+  const float4* tw = G::TW_SMEM ? tw_s : tw_g;
   using TWL = typename std::conditional<G::TW_SMEM, TwShared, TwGlobal>::type;
   int tile = blockIdx.x;
   if (threadIdx.x == 0 && tile < ntiles) {
@@ -320,11 +321,16 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
     if (flags & COL_FWD) {
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = col[slot_pos<N, RF>(t, e) * W];
-      __syncthreads();
-      fft_seq<N, false, SwzAddr, W, TWL>(v, col, t, tw);
+      if constexpr (G::L2) {
+        // the block exchange writes exactly the slots this thread just read: no barrier
+        fft2l_fwd<N, NatAddr, SwzAddr, W, TWL>(v, col, t, tw);
+      } else {
+        __syncthreads();
+        fft_seq<N, false, SwzAddr, W, TWL>(v, col, t, tw);
+      }
     } else {
 #pragma unroll
-      for (int e = 0; e < E; ++e) v[e] = col[slot_pos<N, RX>(t, e) * W];
+      for (int e = 0; e < E; ++e) v[e] = col[col_exit_pos<N, G::L2>(t, e) * W];
       __syncthreads();
     }
     if (flags & (COL_H | COL_MASK)) {
@@ -332,7 +338,7 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
       const float2 exv = ((flags & COL_H) && live) ? __ldg(&a.ex[x]) : make_float2(1.f, 0.f);
 #pragma unroll
       for (int e = 0; e < E; ++e) {
-        const int fy = slot_pos<N, RX>(t, e);
+        const int fy = col_exit_pos<N, G::L2>(t, e);
         const int m = fy < (N + 1) / 2 ? fy : fy - N;
         if ((m < 0 ? -m : m) > lim) {
           v[e] = make_float2(0.f, 0.f);
@@ -343,19 +349,22 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
     }
     if ((flags & COL_SPEC) && live) {
 #pragma unroll
-      for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(slot_pos<N, RX>(t, e)) * nx + x] = v[e];
+      for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(col_exit_pos<N, G::L2>(t, e)) * nx + x] = v[e];
     }
     if (flags & COL_SCALE) {
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = cscale(v[e], a.scale);
     }
     if (flags & COL_INV) {
-      fft_seq<N, true, SwzAddr, W, TWL>(v, col, t, tw);
+      // two-level: the last exchange read exactly the slots this thread writes back
+      if constexpr (G::L2) fft2l_inv<N, NatAddr, SwzAddr, W, TWL>(v, col, t, tw);
+      else fft_seq<N, true, SwzAddr, W, TWL>(v, col, t, tw);
 #pragma unroll
       for (int e = 0; e < E; ++e) col[slot_pos<N, RF>(t, e) * W] = v[e];
     } else {
+      if constexpr (G::L2) __syncthreads();  // other groups may still read their exchange regions
 #pragma unroll
-      for (int e = 0; e < E; ++e) col[slot_pos<N, RX>(t, e) * W] = v[e];
+      for (int e = 0; e < E; ++e) col[col_exit_pos<N, G::L2>(t, e) * W] = v[e];
     }
     fence_async_smem();
     __syncthreads();

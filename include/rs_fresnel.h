@@ -147,6 +147,23 @@ int rs_multislice_plasma(rs_plan* plan, void* u, void* U, const void* ne, const 
                          const double* slice_dz, const double* coord_scale,
                          int slice_begin, int slice_end, void* stream);
 
+/* Multislice through a voxel volume of (delta, beta) float32 pairs per voxel (device,
+ * (nz, ny_v, nx_v, 2)) instead of material ids + table: the same interpolation, transmission
+ * and Fresnel step as rs_multislice_voxel (big-wave/optical_element.py:502-596 with a per-voxel
+ * delta+i*beta). This is the forward model of the adjoint below. */
+int rs_multislice_dbgrid(rs_plan* plan, void* u, void* U, const float* db_grid, const rs_voxel_geom* geom,
+                         double dx, double dy, double wl, double cutoff, const double* slice_dz,
+                         const double* coord_scale, int slice_begin, int slice_end, void* stream);
+
+/* Adjoint of one slice u' = P (t * u) of rs_multislice_dbgrid. On entry v holds P^H g' (g' =
+ * dL/dconj(u'), P^H = a Fresnel step of -dz with the same cutoff); u is the field that entered
+ * the slice. Accumulates dL/d(delta, beta) of the slice's voxels into grad_grid (float32 pairs,
+ * same layout as db_grid) and leaves v = conj(t) * v = dL/dconj(u). No counterpart in the
+ * reference (big-wave has no gradients). */
+int rs_adjoint_slice(rs_plan* plan, void* v, const void* u, const float* db_grid, const rs_voxel_geom* geom,
+                     double dx, double dy, double wl, int slice, double coord_scale, float* grad_grid,
+                     void* stream);
+
 /* Detector geometry (big-wave/propagation.py:766-815 _detector_geometry). */
 typedef struct rs_detector_geom {
   double dx, dy;             /* grid spacings [m]                                      */
@@ -181,6 +198,11 @@ int rs_launch_count(unsigned long long* out);
  * waits for the recorded passes and returns their summed milliseconds and counts, then clears. */
 int rs_plan_profile(rs_plan* plan, int enable);
 int rs_plan_profile_read(rs_plan* plan, double* row_ms, double* col_ms, int* n_row, int* n_col);
+
+/* Adjoint of rs_detector: given r = dL/dI (float64, out_y x out_x, device) and the field u,
+ * writes g = dL/dconj(u) = (D^T r) * u, D the detector integration (area_v1 or legacy). */
+int rs_detector_adjoint(rs_plan* plan, const void* u, void* g, const double* r, const rs_detector_geom* geom,
+                        void* stream);
 
 /* The detector of rs_detector for callers that must not allocate device memory: code that
  * runs where the device memory is owned by someone else (a framework's caching pool, a

@@ -162,6 +162,18 @@ def sample_apply_2d(u, grid, db_list, dx, dy, wl, cutoff, px, py, pz, x_pos=0.0,
     return u, U
 
 
+def dbvolume_apply_2d(u, dbvol, dx, dy, wl, cutoff, px, py, pz, x_pos=0.0, y_pos=0.0):
+    """Sample._apply_2d with a per-voxel delta+i*beta volume (nz, ny_v, nx_v) complex instead of
+    ids + db_list (big-wave/optical_element.py:533-592). Returns (u, U)."""
+    ny, nx = u.shape
+    U = None
+    for z in range(dbvol.shape[0]):
+        db = interpolate_slice(dbvol[z], nx, ny, dx, dy, px, py, x_pos, y_pos)
+        u = (u * material_factor(db, pz, wl)).astype(u.dtype, copy=False)
+        u, U = propagate_2d(u, dx, dy, wl, pz, cutoff)
+    return u, U
+
+
 # ---- plasma (big-wave/plasma.py) ---------------------------------------------------------
 def plasma_delta_beta_grid_multi(ne, ni, te, zstar, f1bar, f2eff_bar, zbar, z2bar, energy,
                                  planck_hc, r_electron_cm):
