@@ -52,6 +52,8 @@ class MultisliceModel:
         self.U = GpuVector(torch.empty(n, dtype=torch.complex64, device=self.device))
         self.checkpoints: dict[int, torch.Tensor] = {}
         self.u_final = None
+        self.last_backward = None  # "fused" (two passes per slice) or "per-slice"
+        self.fused = True          # False forces the per-slice backward
 
     # -- helpers ------------------------------------------------------------------------------
     def _vgeom(self, db: torch.Tensor) -> _lib.VoxelGeom:
@@ -115,6 +117,10 @@ class MultisliceModel:
         # P_final^H
         propagate_2d(g, scratch, p.dx, p.get_dy(), p.wl, -self._final_dz(nz), p.chunk_size, self.cutoff, p.nx, p.ny)
         vg = self._vgeom(db)
+        if self.fused and self._backward_fused(db, g, grad, vg, plan, st):
+            self.last_backward = "fused"
+            return grad
+        self.last_backward = "per-slice"
         for s0 in sorted(self.checkpoints, reverse=True):
             s1 = min(nz, s0 + self.every)
             # recompute the fields entering slices s0 .. s1-1 from the checkpoint
@@ -132,6 +138,35 @@ class MultisliceModel:
                                                     _lib.ptr(db), vg, dx, dy, float(p.wl), k, 1.0, _lib.ptr(grad), st),
                                "rs_adjoint_slice")
         return grad
+
+
+    def _backward_fused(self, db, g, grad, vg, plan, st) -> bool:
+        """Backward sweep in two fused passes per slice (rs_adjoint_multislice_dbgrid), each segment's
+        fields recomputed from its checkpoint by rs_multislice_dbgrid_store. False when the size is
+        not supported by the fused kernels (the caller then takes the per-slice path)."""
+        p = self.p
+        lib = _lib.lib()
+        nz = db.shape[0]
+        n = p.nx * p.ny
+        dz = _lib.doubles(self._dz(nz))
+        fields = torch.empty((self.every, n), dtype=torch.complex64, device=self.device)
+        for s0 in sorted(self.checkpoints, reverse=True):
+            s1 = min(nz, s0 + self.every)
+            self.u.vec.copy_(self.checkpoints[s0])
+            with torch.cuda.device(self.device):
+                rc = lib.rs_multislice_dbgrid_store(plan.handle, _lib.ptr(self.u.vec), _lib.ptr(self.U.vec),
+                                                    _lib.ptr(db), vg, float(p.dx), float(p.get_dy()), float(p.wl),
+                                                    self.cutoff, dz, None, s0, s1, _lib.ptr(fields), st)
+                if rc == _lib.RS_EUNSUPPORTED:
+                    return False
+                _lib.check(rc, "rs_multislice_dbgrid_store")
+                rc = lib.rs_adjoint_multislice_dbgrid(plan.handle, _lib.ptr(g.vec), _lib.ptr(db), vg, float(p.dx),
+                                                      float(p.get_dy()), float(p.wl), self.cutoff, dz, None, s0, s1,
+                                                      _lib.ptr(fields), _lib.ptr(grad), st)
+                if rc == _lib.RS_EUNSUPPORTED:
+                    return False
+                _lib.check(rc, "rs_adjoint_multislice_dbgrid")
+        return True
 
 
 class _MultisliceIntensity(torch.autograd.Function):

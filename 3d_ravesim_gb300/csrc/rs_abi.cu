@@ -88,6 +88,14 @@ struct rs_plan {
   float* yf = nullptr;
   void* det = nullptr;
   size_t det_cap = 0;
+  // Geometry whose forward detector tables sit in `det` (valid = false after any other use of the
+  // buffer). A repeated geometry needs neither the host build nor the copy; the copy matters,
+  // because a pageable host->device copy first waits for all earlier work on its stream.
+  struct DetCache {
+    bool valid = false;
+    rs_detector_geom g{};
+    size_t off[8] = {};
+  } det_cache;
   // pipelined (bulk-copy) passes per direction; RS_PIPELINE / rs_plan_set_pipeline select them
   bool pipe_rows = true;
   bool pipe_cols = true;
@@ -191,7 +199,8 @@ const CUtensorMap* field_map(rs_plan* p, const void* base, int w, int bh) {
 }
 
 cudaError_t run_row(rs_plan* p, const RowArgs& r, cudaStream_t s) {
-  if (p->pipe_rows && row_pipe_ok(p->nx) && (r.flags & ROW_SRC || aligned16(r.in)) && aligned16(r.out))
+  if (p->pipe_rows && !(r.flags & ROW_STORE_U) && row_pipe_ok(p->nx) && (r.flags & ROW_SRC || aligned16(r.in)) &&
+      aligned16(r.out))
     return launch_row_pipe(p->nx, r, p->status, s);
   return launch_row_pass(p->nx, r, s);
 }
@@ -287,6 +296,7 @@ struct SliceSource {
   const char* pg[4] = {nullptr, nullptr, nullptr, nullptr};  // plasma grids
   int f64 = 1;
   PlasmaArgs pl_base{};
+  float2* store = nullptr;     // optional: the field entering slice z goes to store + (z - s0) * nx * ny
 };
 
 // Shared driver of the voxel and plasma multislice entry points.
@@ -347,6 +357,10 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       RowArgs r{};
       r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tws_x; r.ax = axis_tab(p);
       r.flags = (z == s0 ? 0 : ROW_INV) | ROW_FWD | (src.plasma ? ROW_TPLASMA : ROW_TVOX);
+      if (src.store) {
+        r.flags |= ROW_STORE_U;
+        r.aux = src.store + static_cast<size_t>(z - s0) * p->nx * p->ny;
+      }
       r.vox = vox;
       r.pl = pl;
       const int er = prof_begin(p, 0, s);
@@ -826,6 +840,79 @@ int rs_multislice_dbgrid(rs_plan* p, void* u, void* U, const float* db_grid, con
                     slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
 }
 
+int rs_multislice_dbgrid_store(rs_plan* p, void* u, void* U, const float* db_grid, const rs_voxel_geom* geom,
+                               double dx, double dy, double wl, double cutoff, const double* slice_dz,
+                               const double* coord_scale, int slice_begin, int slice_end, void* fields,
+                               void* stream) {
+  RS_TRY(check_plan(p));
+  if (!db_grid || !fields) return fail(RS_EINVAL, "db_grid and fields must be device pointers");
+  if (!p->fast) return fail(RS_EUNSUPPORTED, "field storing needs the fused passes (fast sizes)");
+  SliceSource src;
+  src.dbv = reinterpret_cast<const float2*>(db_grid);
+  src.n_db = 1;
+  src.store = static_cast<float2*>(fields);
+  return multislice(p, static_cast<float2*>(u), static_cast<float2*>(U), src, geom, dx, dy, wl, cutoff,
+                    slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
+}
+
+int rs_adjoint_multislice_dbgrid(rs_plan* p, void* g, const float* db_grid, const rs_voxel_geom* geom, double dx,
+                                 double dy, double wl, double cutoff, const double* slice_dz,
+                                 const double* coord_scale, int slice_begin, int slice_end, const void* fields,
+                                 float* grad_grid, void* stream) {
+  RS_TRY(check_plan(p));
+  if (!g || !db_grid || !fields || !grad_grid || !geom || !slice_dz) return fail(RS_EINVAL, "NULL pointer argument");
+  if (geom->nz <= 0 || geom->ny_v < 2 || geom->nx_v < 2) return fail(RS_EINVAL, "bad grid shape");
+  if (slice_begin < 0 || slice_end > geom->nz || slice_begin > slice_end)
+    return fail(RS_EINVAL, "slice range [%d, %d) outside [0, %d]", slice_begin, slice_end, geom->nz);
+  if (!finite_pos(wl)) return fail(RS_EINVAL, "wavelength must be positive");
+  const bool pow2 = (p->nx & (p->nx - 1)) == 0;
+  if (!p->fast || !pow2 || 3 * geom->nx_v > p->nx + p->nx / 16)
+    return fail(RS_EUNSUPPORTED, "fused adjoint needs power-of-two rows with nx_v <= (nx + nx/16)/3");
+  if (slice_begin == slice_end) return RS_OK;
+  cudaStream_t s = as_stream(stream);
+  float2* gv = static_cast<float2*>(g);
+  const size_t plane = static_cast<size_t>(geom->ny_v) * geom->nx_v;
+  const size_t n = static_cast<size_t>(p->nx) * p->ny;
+  const float a = static_cast<float>(geom->pixel_size_z / wl);
+  const float inv_n = static_cast<float>(1.0 / static_cast<double>(n));
+  double cur_dz = NAN, cur_cs = NAN;
+  for (int z = slice_end - 1; z >= slice_begin; --z) {
+    const double dz = slice_dz[z];
+    const double cs = coord_scale ? coord_scale[z] : 1.0;
+    if (!(dz == cur_dz)) {
+      RS_TRY(build_prop(p, dx, dy, wl, -dz, cutoff, true, s));  // P^H: the step of -dz, same cutoff
+      cur_dz = dz;
+    }
+    if (!(cs == cur_cs)) {
+      if (!std::isfinite(cs)) return fail(RS_EINVAL, "coordinate scale of slice %d is not finite", z);
+      RS_TRY(build_axes(p, geom, dx, dy, cs, s));
+      cur_cs = cs;
+    }
+    if (z == slice_end - 1) {
+      RowArgs r{};
+      r.in = gv; r.out = gv; r.ny = p->ny; r.tw = p->tws_x; r.flags = ROW_FWD;
+      RS_CK(run_row(p, r, s));
+    }
+    ColArgs c{};
+    c.in = gv; c.out = gv; c.spec = nullptr; c.nx = p->nx; c.tw = p->tws_y;
+    c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
+    c.flags = COL_FWD | COL_H | COL_SCALE | COL_INV;
+    RS_CK(run_col(p, c, s));
+    RowArgs r{};
+    r.in = gv; r.out = gv; r.ny = p->ny; r.tw = p->tws_x; r.ax = axis_tab(p);
+    r.flags = ROW_INV | (z > slice_begin ? ROW_FWD : 0);
+    r.vox.dbv = reinterpret_cast<const float2*>(db_grid) + plane * z;
+    r.vox.nxv = geom->nx_v;
+    r.vox.nyv = geom->ny_v;
+    r.vox.n_db = 1;
+    r.vox.a = a;
+    r.aux = const_cast<float2*>(static_cast<const float2*>(fields)) + static_cast<size_t>(z - slice_begin) * n;
+    r.grad = grad_grid + plane * z * 2;
+    RS_CK(launch_row_adjoint(p->nx, r, s));
+  }
+  return RS_OK;
+}
+
 int rs_adjoint_slice(rs_plan* p, void* v, const void* u, const float* db_grid, const rs_voxel_geom* g,
                      double dx, double dy, double wl, int slice, double coord_scale, float* grad_grid,
                      void* stream) {
@@ -910,6 +997,7 @@ int rs_detector_adjoint(rs_plan* p, const void* u, void* g_out, const double* r,
   put(o_yptr, yptr.data(), yptr.size() * 4);
   put(o_ydet, ydet.data(), ydet.size() * 4);
   cudaStream_t s = as_stream(stream);
+  p->det_cache.valid = false;  // the buffer now holds the transposed tables
   if (total > p->det_cap) {
     if (p->det) RS_CK(cudaFree(p->det));
     p->det = nullptr;
@@ -969,58 +1057,68 @@ int rs_detector(rs_plan* p, const void* u, double* out, const rs_detector_geom* 
   if (!finite_pos(g->dx) || !finite_pos(g->dy) || !finite_pos(g->ds_px) || !finite_pos(g->ds_py))
     return fail(RS_EINVAL, "detector and grid spacings must be positive");
   if (!std::isfinite(g->detector_z) || g->detector_z == 0.0) return fail(RS_EINVAL, "detector z must be finite and non-zero");
-  DetTables t;
-  if (g->integrator == 0) build_area_v1(p->nx, p->ny, *g, t);
-  else if (g->integrator == 1) build_legacy(p->nx, p->ny, *g, t);
-  else return fail(RS_EINVAL, "unknown integrator %d", g->integrator);
-  const size_t o_xdet = 0;
-  const size_t o_ydet = o_xdet + align8(t.xdet.size() * 8);
-  const size_t o_yw = o_ydet + align8(t.ydet.size() * 8);
-  const size_t o_xw = o_yw + align8(t.yw.size() * 8);
-  const size_t o_xptr = o_xw + align8(t.xw.size() * 4);
-  const size_t o_xcell = o_xptr + align8(t.xptr.size() * 4);
-  const size_t o_yptr = o_xcell + align8(t.xcell.size() * 4);
-  const size_t o_ycell = o_yptr + align8(t.yptr.size() * 4);
-  const size_t total = o_ycell + align8(t.ycell.size() * 4) + 8;
-  std::vector<char> host(total, 0);
-  auto put = [&](size_t off, const void* src, size_t n) { if (n) std::memcpy(host.data() + off, src, n); };
-  put(o_xdet, t.xdet.data(), t.xdet.size() * 8);
-  put(o_ydet, t.ydet.data(), t.ydet.size() * 8);
-  put(o_yw, t.yw.data(), t.yw.size() * 8);
-  put(o_xw, t.xw.data(), t.xw.size() * 4);
-  put(o_xptr, t.xptr.data(), t.xptr.size() * 4);
-  put(o_xcell, t.xcell.data(), t.xcell.size() * 4);
-  put(o_yptr, t.yptr.data(), t.yptr.size() * 4);
-  put(o_ycell, t.ycell.data(), t.ycell.size() * 4);
+  if (g->integrator != 0 && g->integrator != 1) return fail(RS_EINVAL, "unknown integrator %d", g->integrator);
   cudaStream_t s = as_stream(stream);
-  if (total > p->det_cap) {
-    if (p->det) RS_CK(cudaFree(p->det));  // cudaFree waits for work still using the old buffer
-    p->det = nullptr;
-    p->det_cap = 0;
-    cudaError_t e = cudaMalloc(&p->det, total);
-    if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc(%zu) for detector tables: %s", total, cudaGetErrorString(e));
-    p->det_cap = total;
+  rs_detector_geom key = *g;
+  key.accumulate = 0;  // does not enter the tables
+  auto& dc = p->det_cache;
+  if (!(dc.valid && std::memcmp(&dc.g, &key, sizeof(key)) == 0)) {
+    dc.valid = false;
+    DetTables t;
+    if (g->integrator == 0) build_area_v1(p->nx, p->ny, *g, t);
+    else build_legacy(p->nx, p->ny, *g, t);
+    size_t* o = dc.off;
+    o[0] = 0;                                     // xdet
+    o[1] = o[0] + align8(t.xdet.size() * 8);      // ydet
+    o[2] = o[1] + align8(t.ydet.size() * 8);      // yw
+    o[3] = o[2] + align8(t.yw.size() * 8);        // xw
+    o[4] = o[3] + align8(t.xw.size() * 4);        // xptr
+    o[5] = o[4] + align8(t.xptr.size() * 4);      // xcell
+    o[6] = o[5] + align8(t.xcell.size() * 4);     // yptr
+    o[7] = o[6] + align8(t.yptr.size() * 4);      // ycell
+    const size_t total = o[7] + align8(t.ycell.size() * 4) + 8;
+    std::vector<char> host(total, 0);
+    auto put = [&](size_t off, const void* src, size_t n) { if (n) std::memcpy(host.data() + off, src, n); };
+    put(o[0], t.xdet.data(), t.xdet.size() * 8);
+    put(o[1], t.ydet.data(), t.ydet.size() * 8);
+    put(o[2], t.yw.data(), t.yw.size() * 8);
+    put(o[3], t.xw.data(), t.xw.size() * 4);
+    put(o[4], t.xptr.data(), t.xptr.size() * 4);
+    put(o[5], t.xcell.data(), t.xcell.size() * 4);
+    put(o[6], t.yptr.data(), t.yptr.size() * 4);
+    put(o[7], t.ycell.data(), t.ycell.size() * 4);
+    if (total > p->det_cap) {
+      if (p->det) RS_CK(cudaFree(p->det));  // cudaFree waits for work still using the old buffer
+      p->det = nullptr;
+      p->det_cap = 0;
+      cudaError_t e = cudaMalloc(&p->det, total);
+      if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc(%zu) for detector tables: %s", total, cudaGetErrorString(e));
+      p->det_cap = total;
+    }
+    // Pageable host->device copies are staged before cudaMemcpyAsync returns, so `host` may be
+    // released now; the kernel is ordered after the copy on the same stream.
+    RS_CK(cudaMemcpyAsync(p->det, host.data(), total, cudaMemcpyHostToDevice, s));
+    dc.g = key;
+    dc.valid = true;
   }
+  const size_t* o = dc.off;
   char* d = static_cast<char*>(p->det);
-  RS_CK(cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, s));
   DetArgs a{};
   a.u = static_cast<const float2*>(u);
   a.out = out;
   a.nx = p->nx;
   a.out_x = g->out_x;
   a.out_y = g->out_y;
-  a.xdet = reinterpret_cast<const double*>(d + o_xdet);
-  a.ydet = reinterpret_cast<const double*>(d + o_ydet);
-  a.yw = reinterpret_cast<const double*>(d + o_yw);
-  a.xw = reinterpret_cast<const float*>(d + o_xw);
-  a.xptr = reinterpret_cast<const int*>(d + o_xptr);
-  a.xcell = reinterpret_cast<const int*>(d + o_xcell);
-  a.yptr = reinterpret_cast<const int*>(d + o_yptr);
-  a.ycell = reinterpret_cast<const int*>(d + o_ycell);
+  a.xdet = reinterpret_cast<const double*>(d + o[0]);
+  a.ydet = reinterpret_cast<const double*>(d + o[1]);
+  a.yw = reinterpret_cast<const double*>(d + o[2]);
+  a.xw = reinterpret_cast<const float*>(d + o[3]);
+  a.xptr = reinterpret_cast<const int*>(d + o[4]);
+  a.xcell = reinterpret_cast<const int*>(d + o[5]);
+  a.yptr = reinterpret_cast<const int*>(d + o[6]);
+  a.ycell = reinterpret_cast<const int*>(d + o[7]);
   a.z = g->detector_z;
   a.accumulate = g->accumulate;
-  // Pageable host->device copies are staged before cudaMemcpyAsync returns, so `host` may be
-  // released now; the kernel is ordered after the copy on the same stream.
   RS_CK(launch_detector(a, s));
   return RS_OK;
 }

@@ -17,14 +17,27 @@ namespace rs {
 #define RS_PACKED_F32X2 1
 #endif
 #if RS_PACKED_F32X2 && defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+#define RS_PACKED 1
+#else
+#define RS_PACKED 0
+#endif
+#if RS_PACKED
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return __fmul2_rn(a, make_float2(s, s)); }
+// Complex products as two packed operations: a*b = a.x*(b.x, b.y) + a.y*(-b.y, b.x); each lane is
+// an IEEE multiply then an IEEE fused multiply-add.
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+  return __ffma2_rn(make_float2(a.y, a.y), make_float2(-b.y, b.x), __fmul2_rn(make_float2(a.x, a.x), b));
+}
+// a * conj(b) = a.x*(b.x, -b.y) + a.y*(b.y, b.x)
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
+  return __ffma2_rn(make_float2(a.y, a.y), make_float2(b.y, b.x), __fmul2_rn(make_float2(a.x, a.x), make_float2(b.x, -b.y)));
+}
 #else
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
-#endif
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
@@ -32,6 +45,7 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
 __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, a.y * b.y), fmaf(a.y, b.x, -a.x * b.y));
 }
+#endif
 
 // Compensated twiddles. A twiddle rounded to float carries the same relative error (~3e-8)
 // into every transform of every slice, so over hundreds of slice-steps those errors add up
@@ -39,6 +53,19 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 // (float4 {hi.x, hi.y, lo.x, lo.y}, lo the float nearest to the FP64 rounding residual,
 // hi + lo exact to ~2^-48) and a * w is formed as a*lo + a*hi, the small product first, so
 // that only the final roundings, which depend on a, remain.
+#if RS_PACKED
+__device__ __forceinline__ float2 cmul_tw(float2 a, float4 w) {
+  const float2 ax = make_float2(a.x, a.x), ay = make_float2(a.y, a.y);
+  const float2 c = __ffma2_rn(ay, make_float2(-w.w, w.z), __fmul2_rn(ax, make_float2(w.z, w.w)));
+  return __ffma2_rn(ax, make_float2(w.x, w.y), __ffma2_rn(ay, make_float2(-w.y, w.x), c));
+}
+// a * conj(w)
+__device__ __forceinline__ float2 cmulc_tw(float2 a, float4 w) {
+  const float2 ax = make_float2(a.x, a.x), ay = make_float2(a.y, a.y);
+  const float2 c = __ffma2_rn(ay, make_float2(w.w, w.z), __fmul2_rn(ax, make_float2(w.z, -w.w)));
+  return __ffma2_rn(ax, make_float2(w.x, -w.y), __ffma2_rn(ay, make_float2(w.y, w.x), c));
+}
+#else
 __device__ __forceinline__ float2 cmul_tw(float2 a, float4 w) {
   const float cr = fmaf(a.x, w.z, -a.y * w.w);
   const float ci = fmaf(a.x, w.w, a.y * w.z);
@@ -50,8 +77,16 @@ __device__ __forceinline__ float2 cmulc_tw(float2 a, float4 w) {
   const float ci = fmaf(a.y, w.z, -a.x * w.w);
   return make_float2(fmaf(a.x, w.x, fmaf(a.y, w.y, cr)), fmaf(a.y, w.x, fmaf(-a.x, w.y, ci)));
 }
-// x * (hi + lo) for a real constant split the same way
+#endif
+// x * (hi + lo) for a real constant split the same way, per lane of a pair
 __device__ __forceinline__ float mulk(float x, float hi, float lo) { return fmaf(hi, x, lo * x); }
+__device__ __forceinline__ float2 mulk2(float2 x, float hi, float lo) {
+#if RS_PACKED
+  return __ffma2_rn(make_float2(hi, hi), x, __fmul2_rn(make_float2(lo, lo), x));
+#else
+  return make_float2(mulk(x.x, hi, lo), mulk(x.y, hi, lo));
+#endif
+}
 // multiply by -i (forward) or +i (inverse)
 template <bool INV>
 __device__ __forceinline__ float2 mul_mi(float2 a) {
@@ -75,13 +110,13 @@ __device__ __forceinline__ float2 tw16(float2 a) {
   } else if constexpr (M == 4) {
     return mul_mi<INV>(a);
   } else if constexpr (M == 2) {
-    // fwd: c(1 - i); inv: c(1 + i)
-    return INV ? make_float2(mulk(a.x - a.y, kR2, kR2lo), mulk(a.x + a.y, kR2, kR2lo))
-               : make_float2(mulk(a.x + a.y, kR2, kR2lo), mulk(a.y - a.x, kR2, kR2lo));
+    // fwd: c(1 - i) a = c(x + y, y - x); inv: c(1 + i) a = c(x - y, x + y)
+    return INV ? mulk2(cadd(make_float2(a.x, a.x), make_float2(-a.y, a.y)), kR2, kR2lo)
+               : mulk2(cadd(a, make_float2(a.y, -a.x)), kR2, kR2lo);
   } else if constexpr (M == 6) {
-    // fwd: c(-1 - i); inv: c(-1 + i)
-    return INV ? make_float2(-mulk(a.x + a.y, kR2, kR2lo), mulk(a.x - a.y, kR2, kR2lo))
-               : make_float2(mulk(a.y - a.x, kR2, kR2lo), -mulk(a.x + a.y, kR2, kR2lo));
+    // fwd: c(-1 - i) a = c(y - x, -x - y); inv: c(-1 + i) a = c(-x - y, x - y)
+    return INV ? mulk2(cadd(make_float2(-a.x, a.x), make_float2(-a.y, -a.y)), kR2, kR2lo)
+               : mulk2(cadd(make_float2(-a.x, -a.x), make_float2(a.y, -a.y)), kR2, kR2lo);
   } else {
     // generic: M in {1, 3, 9}
     constexpr float wr = (M == 1) ? kC8 : (M == 3) ? kS8 : -kC8;
@@ -163,8 +198,7 @@ __device__ __forceinline__ void dft3(float2& a0, float2& a1, float2& a2) {
   const float2 t = cadd(a1, a2);
   const float2 d = csub(a1, a2);
   const float2 m = make_float2(fmaf(-0.5f, t.x, a0.x), fmaf(-0.5f, t.y, a0.y));
-  const float2 md = mul_mi<INV>(d);
-  const float2 q = make_float2(mulk(md.x, kHalfSqrt3, kHalfSqrt3lo), mulk(md.y, kHalfSqrt3, kHalfSqrt3lo));
+  const float2 q = mulk2(mul_mi<INV>(d), kHalfSqrt3, kHalfSqrt3lo);
   a0 = cadd(a0, t);
   a1 = cadd(m, q);
   a2 = csub(m, q);

@@ -15,6 +15,10 @@ cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s) {
   return is_pow2(nx) ? launch_row_pass_pow2(nx, a, s) : launch_row_pass_pow3(nx, a, s);
 }
 
+cudaError_t launch_row_adjoint(int nx, const RowArgs& a, cudaStream_t s) {
+  return is_pow2(nx) ? launch_row_adjoint_pow2(nx, a, s) : cudaErrorInvalidValue;
+}
+
 cudaError_t launch_col_pass(int ny, const ColArgs& a, cudaStream_t s) {
   return is_pow2(ny) ? launch_col_pass_pow2(ny, a, s) : launch_col_pass_pow3(ny, a, s);
 }

@@ -74,15 +74,28 @@ __device__ __forceinline__ int padi(int i) { return i + (i >> 4); }
 // PadAddr: one pad per 16 elements (buffers of FftPlan::S elements).
 // SwzAddr: XOR swizzle of p within its 16-element group (dense buffers of N elements, as
 // filled by bulk copies); conflict-free for all power-of-two exchange patterns.
+// at_plus(base, pb, off, base16) is at(base + off) given pb = at(base); off and base16 are
+// compile-time constants after unrolling, and where the policy is affine in off the address
+// is pb plus an immediate (base16: base is a multiple of 16).
 struct PadAddr {
   static __device__ __forceinline__ int at(int p) { return padi(p); }
+  static __device__ __forceinline__ int at_plus(int base, int pb, int off, bool base16) {
+    if (off % 16 == 0) return pb + off + off / 16;
+    if (base16 && off >= 0 && off < 16) return pb + off;
+    return padi(base + off);
+  }
 };
 struct SwzAddr {
   static __device__ __forceinline__ int at(int p) { return p ^ ((p >> 4) & 15); }
+  static __device__ __forceinline__ int at_plus(int base, int pb, int off, bool) {
+    if (off % 256 == 0) return pb + off;  // bits 4..7, which pick the swizzle, are unchanged
+    return at(base + off);
+  }
 };
 // NatAddr: natural order (the layout bulk copies fill and drain).
 struct NatAddr {
   static __device__ __forceinline__ int at(int p) { return p; }
+  static __device__ __forceinline__ int at_plus(int, int pb, int off, bool) { return pb + off; }
 };
 
 // Position held by register e of thread t in a radix-R mapping.
@@ -137,13 +150,15 @@ struct FftStages {
 #pragma unroll
       for (int b = 0; b < B; ++b) {
         const int j = t + b * T;
-        const int base = (j / NS) * NS * R + (j % NS);
+        const int base = (j / NS) * NS * R + (j % NS);  // a multiple of 16 when NS == 1, R == 16
+        const int pb = AD::at(base);
 #pragma unroll
-        for (int q = 0; q < R; ++q) buf[AD::at(base + q * NS) * STR] = v[b * R + q];
+        for (int q = 0; q < R; ++q) buf[AD::at_plus(base, pb, q * NS, NS == 1 && R % 16 == 0) * STR] = v[b * R + q];
       }
       if constexpr (WARP) __syncwarp(); else __syncthreads();
+      const int pt = AD::at(t);
 #pragma unroll
-      for (int e = 0; e < E; ++e) v[e] = buf[AD::at(slot_pos<N, R2>(t, e)) * STR];
+      for (int e = 0; e < E; ++e) v[e] = buf[AD::at_plus(t, pt, slot_pos<N, R2>(0, e), false) * STR];
       if constexpr (!WARP) __syncthreads();
       FftStages<N, INV, SI + 1, NS * R, AD, STR, TWL, WARP>::run(v, buf, t, tw);
     }
@@ -200,13 +215,15 @@ __device__ __forceinline__ void fft2l_fwd(float2 (&v)[16], float2* buf, int t, c
   dft16<false>(v);
 #pragma unroll
   for (int c = 1; c < 16; ++c) v[c] = cmul_tw(v[c], TWL::load(&tw[(c - 1) * T + t]));
+  const int pt = BX::at(t);
 #pragma unroll
-  for (int c = 0; c < 16; ++c) buf[BX::at(c * T + t) * STR] = v[c];
+  for (int c = 0; c < 16; ++c) buf[BX::at_plus(t, pt, c * T, false) * STR] = v[c];
   __syncthreads();
   const int c = t / G;
   const int j = t % G;
+  const int pg = BX::at(c * T + j);
 #pragma unroll
-  for (int e = 0; e < 16; ++e) v[e] = buf[BX::at(c * T + j + e * G) * STR];
+  for (int e = 0; e < 16; ++e) v[e] = buf[BX::at_plus(c * T + j, pg, e * G, false) * STR];
   FftStages<T, false, 0, 1, AD, STR, TWL, true>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T);
 }
 
@@ -219,11 +236,13 @@ __device__ __forceinline__ void fft2l_inv(float2 (&v)[16], float2* buf, int t, c
   const int j = t % G;
   FftStages<T, true, 0, 1, AD, STR, TWL, true>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T);
   __syncwarp();
+  const int pg = BX::at(c * T + j);
 #pragma unroll
-  for (int e = 0; e < 16; ++e) buf[BX::at(c * T + j + e * G) * STR] = v[e];
+  for (int e = 0; e < 16; ++e) buf[BX::at_plus(c * T + j, pg, e * G, false) * STR] = v[e];
   __syncthreads();
+  const int pt = BX::at(t);
 #pragma unroll
-  for (int k = 0; k < 16; ++k) v[k] = buf[BX::at(k * T + t) * STR];
+  for (int k = 0; k < 16; ++k) v[k] = buf[BX::at_plus(t, pt, k * T, false) * STR];
 #pragma unroll
   for (int k = 1; k < 16; ++k) v[k] = cmulc_tw(v[k], TWL::load(&tw[(k - 1) * T + t]));
   dft16<true>(v);

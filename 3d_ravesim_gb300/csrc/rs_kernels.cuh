@@ -19,6 +19,7 @@ enum RowFlags : int {
   ROW_TVOX = 8,     // voxel-Sample transmission between the transforms
   ROW_TPLASMA = 16, // PlasmaSample transmission between the transforms
   ROW_SCALE = 32,   // multiply the stored values by `scale`
+  ROW_STORE_U = 64, // store the spatial row entering the transmission to `aux`
 };
 
 enum ColFlags : int {
@@ -81,6 +82,8 @@ struct RowArgs {
   VoxelArgs vox;
   PlasmaArgs pl;
   PointSrcArgs ps;
+  float2* aux;           // ROW_STORE_U: the fields entering the slice; adjoint: read from here
+  float* grad;           // adjoint: dL/d(delta, beta) of the slice, float pairs per voxel
 };
 
 struct ColArgs {
@@ -101,9 +104,21 @@ struct ColArgs {
 __device__ __forceinline__ float2 material_factor(float delta, float beta, float a) {
   // exp(-2*pi*i*a*conj(delta + i*beta)) = exp(-2*pi*a*beta) * exp(-2*pi*i*a*delta)
   // (big-wave/optical_element.py:39-42)
-  float s, c;
-  sincospif(2.0f * a * delta, &s, &c);
-  const float amp = expf(-6.283185307179586f * a * beta);
+  // Both factors are close to 1 for the usual thin slices, and their rounding repeats in every
+  // slice of similar material, so each is formed so that its only large rounding is the final,
+  // unbiased one to nearest: cos(phi) = 1 - 2 sin^2(phi/2), sin(phi) = 2 sin(phi/2) cos(phi/2)
+  // from the half angle phi/2 = pi*a*delta, and exp(x) = 1 + expm1(x).
+  float sh, ch;
+  sincospif(a * delta, &sh, &ch);
+  const float c = fmaf(-2.0f * sh, sh, 1.0f);
+  const float s = 2.0f * sh * ch;
+  const float x = -6.283185307179586f * a * beta;
+  // expm1 by its Taylor series through x^4 when |x| < 1/64 (remainder below x^5/120 < 1e-11 |x|),
+  // the library expm1f otherwise
+  const float em1 = fabsf(x) < 0.015625f
+                        ? x * fmaf(x, fmaf(x, fmaf(x, 0.041666666666666667f, 0.16666666666666667f), 0.5f), 1.0f)
+                        : expm1f(x);
+  const float amp = 1.0f + em1;
   return make_float2(amp * c, -amp * s);
 }
 
@@ -321,9 +336,10 @@ __device__ __forceinline__ float2 point_source_value(const PointSrcArgs& p, int 
 
 // ----------------------------------------------------------------------------- row pass
 #ifndef RS_ROW_MINB
-#define RS_ROW_MINB 3
+#define RS_ROW_MINB 4
 #endif
-// blocks per SM the row pass's registers are sized for (one 256-thread row block: 3 -> <= 85 regs)
+// blocks per SM the row pass's registers are sized for (one 256-thread row block: 4 -> <= 64
+// registers; the few spilled values cost less than the warps a fourth block adds)
 template <int N, int ROWS>
 constexpr int row_minb() {
   return ROWS * FftPlan<N>::T <= 256 ? (FftPlan<N>::E == 16 ? RS_ROW_MINB : 2) : 1;
@@ -390,6 +406,11 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
       v[e] = valid ? a.in[rbase + slot_pos<N, RF>(t, e)] : make_float2(0.f, 0.f);
   }
 
+  if ((flags & ROW_STORE_U) && valid) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) a.aux[rbase + slot_pos<N, RF>(t, e)] = v[e];
+  }
+
   if (tmode) {
     // The exchange buffer is idle between the two transforms: stage the voxel row blended in y
     // there (one gather per voxel column instead of four per pixel), then interpolate in x.
@@ -425,12 +446,11 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
         if (xi >= 0) {
           const float fx = __int_as_float(xe.y);
           if (staged) {
-            d[i] = buf[xi];
-            if (fx != 0.0f) d[i] = lerp2(d[i], buf[xi + 1], fx);
+            d[i] = lerp2(buf[xi], buf[xi + 1], fx);  // exact for fx = 0; xi + 1 < nxv
           } else {
             d[i] = vox ? voxel_db(a.vox, xi, fx, yi, fy) : plasma_db(a.pl, xi, fx, yi, fy);
           }
-          any |= (d[i].x != 0.0f) | (d[i].y != 0.0f);
+          any |= ((__float_as_uint(d[i].x) | __float_as_uint(d[i].y)) << 1) != 0u;  // +-0 is vacuum
         }
       }
       if (__any_sync(0xffffffffu, any)) {
@@ -460,6 +480,102 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   }
 }
 
+// ------------------------------------------------------------------ adjoint row pass
+// The adjoint of one slice fused between the row transforms of the backward sweep:
+// [row IFFT] -> v = P^H g' in the spatial domain; with u the field that entered the slice (aux)
+// and t its transmission, accumulate dL/ddelta = 4 pi a Im(t conj(G)), dL/dbeta =
+// -4 pi a Re(t conj(G)), G = conj(u) v, through the bilinear weights into `grad`, and continue
+// with conj(t) v -> [row FFT]. The y-blended (delta, beta) row and the two voxel rows' gradient
+// sums live in the exchange buffer (3 nxv float pairs; the host checks nxv <= S/3), and each
+// block adds its sums to the grid with one global atomic per touched value.
+template <int N, int ROWS>
+__global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row_adjoint_kernel(const RowArgs a) {
+  using P = FftPlan<N>;
+  constexpr int T = P::T;
+  constexpr int E = P::E;
+  constexpr int RF = P::entry_radix(false);
+  constexpr int RX = P::exit_radix(false);
+  extern __shared__ float2 smem[];
+  const int t = threadIdx.x % T;
+  const int lr = threadIdx.x / T;
+  const int row = blockIdx.x * ROWS + lr;
+  const bool valid = row < a.ny;
+  float2* buf = smem + lr * P::S;
+  const size_t rbase = static_cast<size_t>(valid ? row : 0) * N;
+  const int flags = a.flags;
+  const int nxv = a.vox.nxv;
+  float2 v[E];
+  int yi = -1;
+  float fy = 0.0f;
+  if (valid) {
+    yi = __ldg(&a.ax.yi[row]);
+    if (yi >= 0) fy = __ldg(&a.ax.yf[row]);
+  }
+  if (flags & ROW_INV) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = valid ? a.in[rbase + slot_pos<N, RX>(t, e)] : make_float2(0.f, 0.f);
+    fft_seq<N, true>(v, buf, t, a.tw);
+  } else {
+#pragma unroll
+    for (int e = 0; e < E; ++e) v[e] = valid ? a.in[rbase + slot_pos<N, RF>(t, e)] : make_float2(0.f, 0.f);
+  }
+  float* acc = reinterpret_cast<float*>(buf + nxv);  // [2 rows][nxv][delta, beta]
+  if (yi >= 0) {
+    for (int j = t; j < nxv; j += T) buf[j] = voxel_col_blend(a.vox, j, yi, fy);
+    for (int j = t; j < 4 * nxv; j += T) acc[j] = 0.0f;
+  }
+  __syncthreads();
+  if (yi >= 0) {
+    const float k = 12.566370614359172f * a.vox.a;  // 4 pi t / wl
+    const float gy0 = 1.0f - fy;
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int x = slot_pos<N, RF>(t, e);
+      const int2 xe = __ldg(&a.ax.xp[x]);
+      const int xi = xe.x;
+      if (xi < 0) continue;  // outside the grid: t = 1 and no voxel depends on this pixel
+      const float fx = __int_as_float(xe.y);
+      const float2 d = lerp2(buf[xi], buf[xi + 1], fx);
+      const float2 tr = material_factor(d.x, d.y, a.vox.a);
+      const float2 uu = a.aux[rbase + x];
+      const float2 G = cmulc(v[e], uu);   // conj(u) v
+      const float2 q = cmulc(tr, G);      // t conj(G)
+      const float gd = k * q.y, gb = -k * q.x;
+      const float gx0 = 1.0f - fx;
+      float* r0 = acc + 2 * xi;
+      float* r1 = acc + 2 * (nxv + xi);
+      atomicAdd(r0, gx0 * gy0 * gd);
+      atomicAdd(r0 + 1, gx0 * gy0 * gb);
+      atomicAdd(r0 + 2, fx * gy0 * gd);
+      atomicAdd(r0 + 3, fx * gy0 * gb);
+      atomicAdd(r1, gx0 * fy * gd);
+      atomicAdd(r1 + 1, gx0 * fy * gb);
+      atomicAdd(r1 + 2, fx * fy * gd);
+      atomicAdd(r1 + 3, fx * fy * gb);
+      v[e] = cmulc(v[e], tr);               // conj(t) v
+    }
+  }
+  __syncthreads();
+  if (yi >= 0) {
+    float* g0 = a.grad + static_cast<size_t>(yi) * nxv * 2;  // rows yi and yi + 1 are contiguous
+    for (int j = t; j < 4 * nxv; j += T) {
+      const float val = acc[j];
+      if (val != 0.0f) atomicAdd(&g0[j], val);
+    }
+  }
+  __syncthreads();  // the forward transform reuses the buffer
+  if (flags & ROW_FWD) {
+    fft_seq<N, false>(v, buf, t, a.tw);
+    if (valid) {
+#pragma unroll
+      for (int e = 0; e < E; ++e) a.out[rbase + slot_pos<N, RX>(t, e)] = v[e];
+    }
+  } else if (valid) {
+#pragma unroll
+    for (int e = 0; e < E; ++e) a.out[rbase + slot_pos<N, RF>(t, e)] = v[e];
+  }
+}
+
 // -------------------------------------------------------------------------- column pass
 // W adjacent columns per block; column c of the strip uses its own padded buffer whose
 // stride is offset by 16/W elements so the W columns fall in different banks.
@@ -477,8 +593,12 @@ __device__ __forceinline__ int col_exit_pos(int t, int e) {
   else return slot_pos<N, FftPlan<N>::exit_radix(false)>(t, e);
 }
 
+#ifndef RS_COL_MINB
+#define RS_COL_MINB 1
+#endif
 template <int N, int W>
-__global__ void __launch_bounds__(W * FftPlan<N>::T) col_pass_kernel(const ColArgs a) {
+__global__ void __launch_bounds__(W * FftPlan<N>::T, (W * FftPlan<N>::T <= 512 ? RS_COL_MINB : 1))
+    col_pass_kernel(const ColArgs a) {
   using P = FftPlan<N>;
   constexpr bool L2 = Fft2L<N>::ok(W);  // two-level column transforms (one block barrier each)
   constexpr int RF = P::entry_radix(false);
@@ -547,6 +667,8 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T) col_pass_kernel(const ColAr
 void note_launch(unsigned n = 1);
 
 cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s);
+// Adjoint row pass (row_adjoint_kernel) for power-of-two nx; cudaErrorInvalidValue otherwise.
+cudaError_t launch_row_adjoint(int nx, const RowArgs& a, cudaStream_t s);
 // Compensated stage-major twiddle tables of the fused passes for length n (fast sizes only).
 cudaError_t launch_stage_twiddles(int n, float4* tw, cudaStream_t s);
 int stage_twiddle_len(int n);

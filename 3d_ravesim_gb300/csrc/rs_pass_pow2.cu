@@ -19,6 +19,16 @@ cudaError_t launch_row_pass_pow2(int n, const RowArgs& a, cudaStream_t s) {
   }
 }
 
+#define RS_ROWADJ_CASE(N) \
+  case N: return launch_row_adjoint_n<N>(a, s);
+
+cudaError_t launch_row_adjoint_pow2(int n, const RowArgs& a, cudaStream_t s) {
+  switch (n) {
+    RS_POW2_SIZES(RS_ROWADJ_CASE)
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_col_pass_pow2(int n, const ColArgs& a, cudaStream_t s) {
   switch (n) {
     RS_POW2_SIZES(RS_COL_CASE)

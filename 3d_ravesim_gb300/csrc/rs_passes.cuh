@@ -35,6 +35,27 @@ cudaError_t launch_rows_n(const RowArgs& a, cudaStream_t s) {
   return e;
 }
 
+template <int N>
+cudaError_t launch_row_adjoint_n(const RowArgs& a, cudaStream_t s) {
+  constexpr int ROWS = rows_per_block<N>();
+  constexpr int THREADS = ROWS * FftPlan<N>::T;
+  constexpr size_t SMEM = static_cast<size_t>(ROWS) * FftPlan<N>::S * sizeof(float2);
+  static unsigned configured = 0;  // one bit per device ordinal
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
+  const unsigned bit = 1u << (dev & 31);
+  if (!(configured & bit)) {
+    cudaError_t e = cudaFuncSetAttribute(row_adjoint_kernel<N, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(SMEM));
+    if (e != cudaSuccess) return e;
+    configured |= bit;
+  }
+  row_adjoint_kernel<N, ROWS><<<(a.ny + ROWS - 1) / ROWS, THREADS, SMEM, s>>>(a);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) note_launch();
+  return e;
+}
+
 // exp(-2*pi*i*m/N) evaluated in FP64, split into a float and the float of its residual.
 __device__ __forceinline__ float4 twiddle_fp64(long long m, int n) {
   double sn, cs;
@@ -217,6 +238,7 @@ bool row_pipe_ok_pow3(int n);
 // Per-family dispatchers (rs_pass_pow2.cu / rs_pass_pow3.cu); return cudaErrorInvalidValue
 // for a size outside the family.
 cudaError_t launch_row_pass_pow2(int n, const RowArgs& a, cudaStream_t s);
+cudaError_t launch_row_adjoint_pow2(int n, const RowArgs& a, cudaStream_t s);
 cudaError_t launch_row_pass_pow3(int n, const RowArgs& a, cudaStream_t s);
 cudaError_t launch_col_pass_pow2(int n, const ColArgs& a, cudaStream_t s);
 cudaError_t launch_col_pass_pow3(int n, const ColArgs& a, cudaStream_t s);

@@ -109,19 +109,35 @@ struct ColPipeGeom {
   static constexpr int BH = box_rows(N);                      // rows per tensor-copy box
   static_assert(N % BH == 0, "the boxes must tile a column exactly");
   static constexpr int TILE = W * N;
-  static constexpr int NB = (3 * TILE * 8 <= 200 * 1024) ? 3 : 2;
   static constexpr int THREADS = W * T;
-  // twiddles (forward and inverse stage-major tables) copied to shared memory when they fit
   static constexpr bool L2 = Fft2L<N>::ok(W);                 // two-level column transforms
+  // twiddles (compensated tables) copied to shared memory when they fit
   static constexpr int TW_LEN = L2 ? Fft2L<N>::TW_LEN : FftPlan<N>::TW_USED;
-  static constexpr size_t TILES_BYTES = static_cast<size_t>(NB) * TILE * sizeof(float2);
   static constexpr size_t TW_BYTES = static_cast<size_t>(TW_LEN) * sizeof(float4);
+  // Three tile buffers when they fit beside the twiddle tables, else two: the twiddles in shared
+  // memory matter more than the third buffer (the L1 left beside three 64 KB tiles cannot hold
+  // the compensated tables of 4096-point columns).
+#ifdef RS_COLPIPE_NB
+  static constexpr int NB = RS_COLPIPE_NB;
+#else
+  static constexpr int NB = (3 * TILE * 8 + TW_BYTES + 64 <= 227 * 1024) ? 3 : 2;
+#endif
+  static constexpr size_t TILES_BYTES = static_cast<size_t>(NB) * TILE * sizeof(float2);
 #ifndef RS_COLPIPE_TW_SMEM
 #define RS_COLPIPE_TW_SMEM 1
 #endif
   static constexpr bool TW_SMEM =
       RS_COLPIPE_TW_SMEM && TW_LEN > 0 && TILES_BYTES + TW_BYTES + 64 <= 227 * 1024;
-  static constexpr size_t SMEM = TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + NB * sizeof(uint64_t);
+  // ey in shared memory too when it fits, stored in the register order of the forward exit
+  // mapping (entry e * T + t), so that a warp's reads are consecutive
+#ifndef RS_COLPIPE_EY_SMEM
+#define RS_COLPIPE_EY_SMEM 1
+#endif
+  static constexpr size_t EY_BYTES = static_cast<size_t>(N) * sizeof(float2);
+  static constexpr bool EY_SMEM =
+      RS_COLPIPE_EY_SMEM && TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + EY_BYTES + 64 <= 227 * 1024;
+  static constexpr size_t SMEM =
+      TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + (EY_SMEM ? EY_BYTES : 0) + NB * sizeof(uint64_t);
 };
 
 // ---------------------------------------------------------------------- row pipeline
@@ -276,7 +292,9 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   float2* tiles = reinterpret_cast<float2*>(smem_raw);
   float4* tw_s = reinterpret_cast<float4*>(tiles + G::NB * G::TILE);
-  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + G::TILES_BYTES + (G::TW_SMEM ? G::TW_BYTES : 0));
+  float2* ey_s = reinterpret_cast<float2*>(smem_raw + G::TILES_BYTES + (G::TW_SMEM ? G::TW_BYTES : 0));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + G::TILES_BYTES + (G::TW_SMEM ? G::TW_BYTES : 0) +
+                                               (G::EY_SMEM ? G::EY_BYTES : 0));
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
   const int nx = a.nx;
@@ -295,6 +313,13 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
   }
   const float4* tw = G::TW_SMEM ? tw_s : tw_g;
   using TWL = typename std::conditional<G::TW_SMEM, TwShared, TwGlobal>::type;
+  if constexpr (G::EY_SMEM) {
+    if (flags & COL_H) {  // uniform: a.ey is set whenever H is applied
+      for (int i = threadIdx.x; i < N; i += blockDim.x)
+        ey_s[i] = __ldg(&a.ey[col_exit_pos<N, G::L2>(i % P::T, i / P::T)]);
+    }
+    __syncthreads();
+  }
   int tile = blockIdx.x;
   if (threadIdx.x == 0 && tile < ntiles) {
     mbar_arrive_expect(&bars[0], TILE_BYTES);
@@ -305,13 +330,18 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
     const int b = i % G::NB;
     float2* tb = tiles + b * G::TILE;
     const int next = tile + gridDim.x;
-    if (threadIdx.x == 0 && next < ntiles) {
-      bulk_wait_read<G::NB - 2>();
-      const int bn = (i + 1) % G::NB;
-      mbar_arrive_expect(&bars[bn], TILE_BYTES);
-      for (int k = 0; k < N / G::BH; ++k)
-        tma_load_2d(tiles + bn * G::TILE + k * G::BH * W, &map_in, next * W, k * G::BH, &bars[bn]);
-    }
+    // The next strip goes into the buffer whose store was issued at the end of the previous
+    // iteration; the copy is started halfway through this strip's work (below), by when that
+    // store has long been read out, so no thread waits for it.
+    auto prefetch_next = [&]() {
+      if (threadIdx.x == 0 && next < ntiles) {
+        bulk_wait_read<G::NB - 2>();
+        const int bn = (i + 1) % G::NB;
+        mbar_arrive_expect(&bars[bn], TILE_BYTES);
+        for (int k = 0; k < N / G::BH; ++k)
+          tma_load_2d(tiles + bn * G::TILE + k * G::BH * W, &map_in, next * W, k * G::BH, &bars[bn]);
+      }
+    };
     ok = __syncthreads_and(mbar_wait_bounded(&bars[b], (i / G::NB) & 1, status));
     if (!ok) break;
     const int x = tile * W + c;
@@ -343,10 +373,12 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
         if ((m < 0 ? -m : m) > lim) {
           v[e] = make_float2(0.f, 0.f);
         } else if (flags & COL_H) {
-          v[e] = cmul(v[e], cmul(exv, __ldg(&a.ey[fy])));
+          const float2 eyv = G::EY_SMEM ? ey_s[e * P::T + t] : __ldg(&a.ey[fy]);
+          v[e] = cmul(v[e], cmul(exv, eyv));
         }
       }
     }
+    prefetch_next();
     if ((flags & COL_SPEC) && live) {
 #pragma unroll
       for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(col_exit_pos<N, G::L2>(t, e)) * nx + x] = v[e];

@@ -40,6 +40,11 @@ UNIT = "slice-steps/s"
 PUBLISHED_MS_PER_LAYER = 43.25
 
 
+# DRAM bytes per launch of the fused passes at 4096^2 from one ncu capture of this workload
+# (profiles/row_pass_col_pipe_4096.md: dram__bytes.sum.per_second x gpu__time_duration.sum)
+NCU_DRAM_BYTES_4096 = {"row_pass": 221.5e6, "col_pass": 215.5e6}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -233,8 +238,9 @@ def cpu_baseline(n: int, samples: int = 2) -> dict:
 
 
 def accuracy_check(rs, torch, device, n: int, slices: int = 4) -> dict:
-    """Relative L2 of field and detector intensity vs the FP64 oracle on the benchmark geometry
-    truncated to `slices` sample slices (the full 512-slice FP64 run takes hours on the CPU)."""
+    """Relative L2 of field and detector intensity vs the FP64 oracle on the benchmark geometry at
+    n^2 with `slices` sample slices (a full 512-slice FP64 run at 4096^2 takes hours on the CPU,
+    at 1024^2 about half a minute)."""
     from scipy import fft as spfft
 
     from oracle import bigwave_oracle as orc
@@ -262,10 +268,86 @@ def accuracy_check(rs, torch, device, n: int, slices: int = 4) -> dict:
         u, U = orc.propagate_2d(u, p.dx, p.dx, p.wl, p.z_detector - z, w.cutoff, U=U, skip_fft=True)
     ref_det = orc.detector_area_v1(u, p.dx, p.dx, p.detector_pixel_size_x, p.detector_pixel_size_y,
                                    gpu_det.shape[1], gpu_det.shape[0], p.z_detector)
-    return {"case": f"Talbot-Lau {n}^2 truncated to {slices} sample slices vs FP64 oracle",
+    return {"case": f"Talbot-Lau {n}^2 with {slices} sample slices vs FP64 oracle",
             "field_rel_l2": orc.relative_l2(gpu_u, u),
             "intensity_rel_l2": orc.relative_l2(np.abs(gpu_u) ** 2, np.abs(u) ** 2),
             "detector_rel_l2": orc.relative_l2(gpu_det, ref_det)}
+
+
+def adjoint_cost(rs, torch, device, n: int = 2048, slices: int = 256) -> dict:
+    """Gradient cost of the differentiable plasma workload (2048^2, 8 keV, 256 x 2 um slices of a
+    Gaussian plasma, n0 = 1e21 cm^-3, L = 150 um, T_e = 500 eV): one forward pass against one
+    forward + adjoint (loss L2, gradients to every voxel's delta/beta and to n0, L, T_e)."""
+    adj = importlib.import_module("3d_ravesim_gb300.adjoint")
+    energy, dx, pz, pitch = 8000.0, 0.5e-6, 2e-6, 2e-6
+    wl = rs.convert_energy_wavelength(energy)
+    glen = int(math.ceil(n * dx / pitch)) + 4
+    glen += glen % 2
+    geom = adj.VolumeGeometry(z_start=0.1, pixel_size_x=pitch, pixel_size_y=pitch, pixel_size_z=pz)
+    p = rs.SimParams(N=n * n, nx=n, ny=n, dx=dx, dy=dx, z_detector=0.1 + slices * pz + 0.2, detector_size=n * dx,
+                     detector_pixel_size_x=dx, detector_pixel_size_y=dx, wl=wl, chunk_size=n)
+    u0 = torch.ones(n * n, dtype=torch.complex64, device=device)
+    model = adj.MultisliceModel(p, geom, 0.45 / dx, u0)
+    th = [torch.tensor(v, dtype=torch.float64, device=device, requires_grad=True) for v in (1e21, 150e-6, 500.0)]
+
+    def fwd(params=th):
+        db = adj.gaussian_plasma_db(params[0], params[1], params[2], (slices, glen, glen), (pz, pitch, pitch), energy)
+        return adj.multislice_intensity(db, model)
+    # target: the intensity of slightly different parameters with Poisson noise at 1e4 photons/pixel
+    with torch.no_grad():
+        truth = fwd([torch.tensor(v, dtype=torch.float64, device=device) for v in (1.05e21, 145e-6, 550.0)])
+        scale = 1e4 / truth.mean()
+        gen = torch.Generator(device=device).manual_seed(0)
+        target = torch.poisson(truth * scale, generator=gen) / scale
+
+    def grad():
+        for t in th:
+            t.grad = None
+        ((fwd() - target) ** 2).sum().backward()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    with torch.no_grad():
+        fwd()
+    grad()
+    torch.cuda.synchronize()
+    ev[0].record()
+    with torch.no_grad():
+        fwd()
+    ev[1].record()
+    grad()
+    ev[2].record()
+    ev[2].synchronize()
+    f_ms, g_ms = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    return {"case": f"Gaussian plasma {n}^2, {slices} slices, grid {[slices, glen, glen]}; L2 loss against a "
+            "Poisson-noisy (1e4 photons/pixel) image of n0 = 1.05e21, L = 145 um, T_e = 550 eV",
+            "backward": model.last_backward, "forward_ms": round(f_ms, 2),
+            "forward_plus_gradient_ms": round(g_ms, 2), "ratio": round(g_ms / f_ms, 2),
+            "checkpoint_every": model.every, "grad_n0_L_Te": [float(t.grad) for t in th]}
+
+
+def multisim_cost(rs, torch, device, items: int = 128) -> dict:
+    """Batched multisim (64 jittered sources x 16 Kramers energies, grid sizes from {1024, 1536,
+    2048, 3072}^2, 64-slice shell, 2048^2 area_v1 detector summed incoherently): the first `items`
+    items through the fused multi-stream runner and through the loop of the plain unfused form."""
+    ms = importlib.import_module("3d_ravesim_gb300.multisim")
+    b = ms.shell_batch(max_items=items)
+    fused = ms.BatchRunner(b, device, streams=4)
+    plain = ms.BatchRunner(b, device, streams=1)
+    fused.run(b.items[:4])
+    plain.run(b.items[:1], plain=True)
+    fused.zero()
+    plain.zero()
+    out = {}
+    for name, runner, kw in (("fused", fused, {}), ("plain_loop", plain, {"plain": True})):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        runner.run(**kw)
+        torch.cuda.synchronize()
+        out[name + "_s"] = round(time.perf_counter() - t0, 3)
+    slices = b.sample.grid.shape[0]
+    return {"case": f"{items} of 1024 items, sizes {b.info['sizes']}, {slices} slices each",
+            "fused_items_per_s": round(items / out["fused_s"], 2),
+            "plain_loop_items_per_s": round(items / out["plain_loop_s"], 2),
+            "speedup": round(out["plain_loop_s"] / out["fused_s"], 2), **out}
 
 
 def run_ours(args):
@@ -339,7 +421,9 @@ def run_ours(args):
     achieved = col_gbs if dom == "col_pass" else row_gbs
     roofline = {"bound": "hbm", "kernel": f"{dom} (fused {'column FFT*H*IFFT' if dom == 'col_pass' else 'row IFFT*T*FFT'})",
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "peak_kind": peak_kind, "traffic": None,
+                "peak_kind": peak_kind,
+                "traffic": NCU_DRAM_BYTES_4096[dom] if n == 4096 else None,
+                "traffic_source": "ncu dram bytes per launch, profiles/row_pass_col_pipe_4096.md",
                 "row_pass": {"avg_us": round(row_avg * 1e3, 2), "GB_s": round(row_gbs, 1), "launches": nr.value,
                              "algorithmic_bytes": row_bytes},
                 "col_pass": {"avg_us": round(col_avg * 1e3, 2), "GB_s": round(col_gbs, 1), "launches": nc.value,
@@ -382,8 +466,13 @@ def run_ours(args):
         line["plain"] = {"own_fft_unfused": round(plain, 1), "cufft_unfused": round(cufft, 1),
                          "fused_sample_slices": round(fused_rate, 1) if fused_rate else None, "unit": UNIT,
                          "note": "unfused = T kernel, FFT2, H*mask, IFFT2 as separate launches per slice"}
+        line["adjoint"] = adjoint_cost(rs, torch, device)
+        line["multisim"] = multisim_cost(rs, torch, device)
         line["cpu_baseline"] = cpu_baseline(n)
-        line["accuracy"] = accuracy_check(rs, torch, device, min(n, 4096))
+        # the full slice count at 1024^2 (errors that repeat every slice add up over 514 of them),
+        # and the benchmark size itself truncated to 4 sample slices
+        line["accuracy"] = [accuracy_check(rs, torch, device, 1024, slices=args.slices),
+                            accuracy_check(rs, torch, device, min(n, 4096))]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

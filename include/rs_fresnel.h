@@ -155,6 +155,26 @@ int rs_multislice_dbgrid(rs_plan* plan, void* u, void* U, const float* db_grid, 
                          double dx, double dy, double wl, double cutoff, const double* slice_dz,
                          const double* coord_scale, int slice_begin, int slice_end, void* stream);
 
+/* rs_multislice_dbgrid that also writes the field entering each slice z of [slice_begin,
+ * slice_end) to fields + (z - slice_begin) * nx * ny (complex64, device): the recomputation
+ * step of a checkpointed adjoint. Fast sizes only (RS_EUNSUPPORTED otherwise). */
+int rs_multislice_dbgrid_store(rs_plan* plan, void* u, void* U, const float* db_grid, const rs_voxel_geom* geom,
+                               double dx, double dy, double wl, double cutoff, const double* slice_dz,
+                               const double* coord_scale, int slice_begin, int slice_end, void* fields,
+                               void* stream);
+
+/* Backward sweep of rs_multislice_dbgrid over slices [slice_begin, slice_end) in two fused passes
+ * per slice. On entry g = dL/dconj(u_end), the gradient with respect to the field leaving
+ * slice_end - 1; on exit g = dL/dconj(u_begin). fields holds the fields entering each slice as
+ * written by rs_multislice_dbgrid_store; dL/d(delta, beta) of every slice's voxels is added to
+ * grad_grid (same layout as db_grid). Needs power-of-two rows and nx_v <= (nx + nx/16)/3
+ * (RS_EUNSUPPORTED otherwise; rs_adjoint_slice covers the rest). No counterpart in the reference
+ * (big-wave has no gradients). */
+int rs_adjoint_multislice_dbgrid(rs_plan* plan, void* g, const float* db_grid, const rs_voxel_geom* geom, double dx,
+                                 double dy, double wl, double cutoff, const double* slice_dz,
+                                 const double* coord_scale, int slice_begin, int slice_end, const void* fields,
+                                 float* grad_grid, void* stream);
+
 /* Adjoint of one slice u' = P (t * u) of rs_multislice_dbgrid. On entry v holds P^H g' (g' =
  * dL/dconj(u'), P^H = a Fresnel step of -dz with the same cutoff); u is the field that entered
  * the slice. Accumulates dL/d(delta, beta) of the slice's voxels into grad_grid (float32 pairs,
