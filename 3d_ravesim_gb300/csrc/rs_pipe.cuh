@@ -176,14 +176,18 @@ __global__ void __launch_bounds__(RowPipeGeom<N>::THREADS, RowPipeGeom<N>::MINB)
     const int b = i % G::NB;
     float2* tb = tiles + b * G::TILE;
     const int next = tile + gridDim.x;
-    if (threadIdx.x == 0 && loads && next < ntiles) {
-      bulk_wait_read<G::NB - 2>();  // the buffer's previous store has been read out
-      const int bn = (i + 1) % G::NB;
-      const int r0 = next * G::RW;
-      const uint32_t bytes = static_cast<uint32_t>(min(G::RW, a.ny - r0)) * N * 8u;
-      mbar_arrive_expect(&bars[bn], bytes);
-      bulk_load(tiles + bn * G::TILE, a.in + static_cast<size_t>(r0) * N, bytes, &bars[bn]);
-    }
+    // Started after this tile's first transform (below): by then the store that last used the
+    // target buffer has been read out, so thread 0 does not hold the block up waiting for it.
+    auto prefetch_next = [&]() {
+      if (threadIdx.x == 0 && loads && next < ntiles) {
+        bulk_wait_read<G::NB - 2>();  // the buffer's previous store has been read out
+        const int bn = (i + 1) % G::NB;
+        const int r0n = next * G::RW;
+        const uint32_t bytes = static_cast<uint32_t>(min(G::RW, a.ny - r0n)) * N * 8u;
+        mbar_arrive_expect(&bars[bn], bytes);
+        bulk_load(tiles + bn * G::TILE, a.in + static_cast<size_t>(r0n) * N, bytes, &bars[bn]);
+      }
+    };
     if (loads) {
       ok = mbar_wait_bounded(&bars[b], (i / G::NB) & 1, status);
     } else if (threadIdx.x == 0) {
@@ -210,6 +214,7 @@ __global__ void __launch_bounds__(RowPipeGeom<N>::THREADS, RowPipeGeom<N>::MINB)
       for (int e = 0; e < E; ++e) v[e] = seq[slot_pos<N, RF>(t, e)];
       __syncthreads();
     }
+    prefetch_next();
 
     if (flags & (ROW_TVOX | ROW_TPLASMA)) {
       const bool vox = flags & ROW_TVOX;
@@ -239,16 +244,16 @@ __global__ void __launch_bounds__(RowPipeGeom<N>::THREADS, RowPipeGeom<N>::MINB)
         for (int i = 0; i < CH; ++i) {
           d[i] = make_float2(0.f, 0.f);
           const int x = slot_pos<N, RF>(t, c0 + i);
-          const int xi = yi >= 0 ? __ldg(&a.ax.xi[x]) : -1;
+          const int2 xe = yi >= 0 ? __ldg(&a.ax.xp[x]) : make_int2(-1, 0);
+          const int xi = xe.x;
           if (xi >= 0) {
-            const float fx = __ldg(&a.ax.xf[x]);
+            const float fx = __int_as_float(xe.y);
             if (staged) {
-              d[i] = vrow[xi];
-              if (fx != 0.0f) d[i] = lerp2(d[i], vrow[xi + 1], fx);
+              d[i] = lerp2(vrow[xi], vrow[xi + 1], fx);  // exact for fx = 0; xi + 1 < nxv
             } else {
               d[i] = vox ? voxel_db(a.vox, xi, fx, yi, fy) : plasma_db(a.pl, xi, fx, yi, fy);
             }
-            any |= (d[i].x != 0.0f) | (d[i].y != 0.0f);
+            any |= ((__float_as_uint(d[i].x) | __float_as_uint(d[i].y)) << 1) != 0u;  // +-0 is vacuum
           }
         }
         if (__any_sync(0xffffffffu, any)) {

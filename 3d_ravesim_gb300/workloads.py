@@ -170,3 +170,57 @@ def gaussian_plasma(n: int = 2048, slices: int = 256, dx: float = 0.5e-6, energy
                   detector_size=fov, detector_pixel_size_x=dx, detector_pixel_size_y=dx, wl=wl, chunk_size=n)
     return Workload("gaussian_plasma", p, [sample], cutoff=0.45 / dx, source_xyz=None, z_first=z0,
                     info={"nx": n, "ny": n, "slices": slices, "energy_ev": energy, "grid": [slices, glen, glen]})
+
+
+def capsule_large(n: int = 16384, slices: int = 1024, dx: float = 50e-9, energy: float = 30000.0,
+                  seed: int = 0, pitch: float = 2e-6, pz: float = 0.5e-6, lmax: int = 8,
+                  amplitude: float = 10e-6, z_source: float = 1.0, z_detector_gap: float = 0.3) -> Workload:
+    """Config-4 field: 16384^2 complex64 (2 GiB) at 30 keV, point source 1 m upstream, an
+    ellipsoidal CH capsule shell (semi-axes 400/400/380 um, 15 um wall, delta 2.5e-7, beta
+    1.5e-10) whose outer radius carries a seeded perturbation of real spherical harmonics
+    l = 1..lmax scaled to `amplitude` at its largest, voxelised at `pitch` in x/y with one voxel
+    plane per slice (slices x pz centred on the capsule; at 1024 x 0.5 um the poles beyond
+    +-256 um lie outside the slab), then 0.3 m of free space to the detector."""
+    from scipy.special import lpmv
+    rng = np.random.default_rng(seed)
+    wl = convert_energy_wavelength(energy)
+    fov = n * dx
+    glen = int(math.ceil(fov / pitch)) + 4
+    glen += glen % 2
+    ax = (np.arange(glen) - glen / 2.0) * pitch
+    zc = (np.arange(slices) + 0.5 - slices / 2.0) * pz
+    # perturbation coefficients c_lm, normalised on a coarse (theta, phi) grid
+    coeffs = [(l, m, rng.normal(), rng.uniform(0, 2 * np.pi)) for l in range(1, lmax + 1) for m in range(0, l + 1)]
+
+    def dr(ct, ph):
+        out = np.zeros(np.broadcast(ct, ph).shape)
+        for l, m, c, p0 in coeffs:
+            out += c * lpmv(m, l, ct) * np.cos(m * ph + p0)
+        return out
+    tg, pg = np.meshgrid(np.linspace(-1, 1, 181), np.linspace(0, 2 * np.pi, 361), indexing="ij")
+    scale = amplitude / np.max(np.abs(dr(tg, pg)))
+    a_xy, c_z, wall = 400e-6, 380e-6, 15e-6
+    yy, xx = np.meshgrid(ax, ax, indexing="ij")
+    r_xy2 = xx * xx + yy * yy
+    ph = np.arctan2(yy, xx)
+    grid = np.zeros((slices, glen, glen), dtype=np.uint32)
+    for k in range(slices):
+        r = np.sqrt(r_xy2 + zc[k] ** 2)
+        ct = np.divide(zc[k], r, out=np.zeros_like(r), where=r > 0)
+        st2 = 1.0 - ct * ct
+        rho = 1.0 / np.sqrt(st2 / a_xy ** 2 + ct * ct / c_z ** 2)
+        near = (r <= rho + amplitude) & (r >= rho - wall - amplitude)  # only there can the wall be
+        if near.any():
+            outer = rho[near] + scale * dr(ct[near], ph[near])
+            rn = r[near]
+            grid[k][near] = ((rn <= outer) & (rn >= outer - wall)).astype(np.uint32)
+    z0 = z_source
+    sample = Sample(z_start=z0, pixel_size_x=pitch, pixel_size_z=pz, grid=grid, materials=[Material("CH", 1.0)],
+                    x_positions=np.array([0.0]), pixel_size_y=pitch, y_positions=np.array([0.0]))
+    sample.db_list = np.array([0.0, 2.5e-7 + 1.5e-10j])
+    z_det = z0 + slices * pz + z_detector_gap
+    p = SimParams(N=n * n, nx=n, ny=n, dx=dx, dy=dx, z_detector=z_det, detector_size=fov,
+                  detector_pixel_size_x=1e-6, detector_pixel_size_y=1e-6, wl=wl, chunk_size=n)
+    return Workload("capsule_large", p, [sample], cutoff=0.45 / dx, source_xyz=(0.0, 0.0, 0.0), z_first=z0,
+                    info={"nx": n, "ny": n, "energy_ev": energy, "sample_slices": slices,
+                          "voxel_grid": [slices, glen, glen]})

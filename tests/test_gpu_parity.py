@@ -24,6 +24,7 @@ def host(v, ny, nx):
 
 
 FAST = [(16, 16), (32, 64), (64, 32), (128, 256), (512, 128), (1024, 64), (256, 2048), (4096, 16), (64, 4096),
+        (8192, 32), (32, 8192), (16384, 16), (16, 16384),
         (24, 48), (96, 1536), (3072, 64), (1536, 192), (768, 384), (48, 6144), (12288, 16)]
 GENERIC = [(40, 28), (72, 72), (24, 16), (48, 64), (3, 3), (4, 4)]
 
@@ -212,7 +213,7 @@ def test_sample_checkpoint_callback_path_matches_fused(rs, cuda, golden):
     assert rel_l2(host(u2, ny, nx), host(u1, ny, nx)) < 1e-6
 
 
-@pytest.mark.parametrize("nx,ny,nz", [(256, 256, 12), (512, 256, 5), (384, 192, 4)])
+@pytest.mark.parametrize("nx,ny,nz", [(256, 256, 12), (512, 256, 5), (384, 192, 4), (16384, 64, 3), (64, 16384, 3)])
 def test_sample_fast_sizes_vs_fp64_oracle(rs, cuda, oracle, nx, ny, nz):
     """Shell sample with bilinear (non-aligned) voxels and aligned voxels, both fast-path sizes."""
     rng = np.random.default_rng(nx + nz)
