@@ -357,7 +357,9 @@ struct RowGeom {
   static constexpr size_t SMEM = PF ? BUF + static_cast<size_t>(ROWS) * PF_WORDS * 4 : BUF;
 };
 
-template <int N, int ROWS>
+// VOX = true: the multislice hot path only (optional row IFFT, voxel transmission, row FFT, the
+// optional field store and scale), so the point-source and plasma code is not in the kernel.
+template <int N, int ROWS, bool VOX = false>
 __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row_pass_kernel(const RowArgs a) {
   using P = FftPlan<N>;
   constexpr int T = P::T;
@@ -375,8 +377,8 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   float2 v[E];
 
   // Transmission row coordinates, and the prefetch of its two voxel rows (block-uniform decision).
-  const bool tmode = flags & (ROW_TVOX | ROW_TPLASMA);
-  const bool vox = flags & ROW_TVOX;
+  const bool tmode = VOX || (flags & (ROW_TVOX | ROW_TPLASMA));
+  const bool vox = VOX || (flags & ROW_TVOX);
   int yi = -1;
   float fy = 0.0f;
   bool pf_on = false;
@@ -397,7 +399,7 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
     for (int e = 0; e < E; ++e)
       v[e] = valid ? a.in[rbase + slot_pos<N, RX>(t, e)] : make_float2(0.f, 0.f);
     fft_seq<N, true>(v, buf, t, a.tw);
-  } else if (flags & ROW_SRC) {
+  } else if (!VOX && (flags & ROW_SRC)) {
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = point_source_value(a.ps, slot_pos<N, RF>(t, e), row);
   } else {

@@ -1,23 +1,16 @@
-// rs_pass_pow3.cu — fused pass and twiddle-table instantiations for the 3*2^k sizes.
+// rs_pass_pow3_cols.cu — column-pass and twiddle-table instantiations for the 3*2^k sizes.
 #include "rs_passes.cuh"
 
 namespace rs {
 
-#define RS_ROW_CASE(N) \
-  case N: return launch_rows_n<N>(a, s);
 #define RS_COL_CASE(N) \
   case N: return launch_cols_nw<N, strip_width<N>()>(a, s);
+
 #define RS_TW_CASE(N) \
   case N: return launch_stage_twiddles_n<N>(tw, s);
+
 #define RS_TWLEN_CASE(N) \
   case N: return stage_twiddle_len_n<N>();
-
-cudaError_t launch_row_pass_pow3(int n, const RowArgs& a, cudaStream_t s) {
-  switch (n) {
-    RS_POW3_SIZES(RS_ROW_CASE)
-    default: return cudaErrorInvalidValue;
-  }
-}
 
 cudaError_t launch_col_pass_pow3(int n, const ColArgs& a, cudaStream_t s) {
   switch (n) {
@@ -40,21 +33,11 @@ int stage_twiddle_len_pow3(int n) {
   }
 }
 
-#define RS_ROWPIPE_CASE(N) \
-  case N: return launch_row_pipe_n<N>(a, status, s);
 #define RS_COLPIPE_CASE(N) \
   case N: return launch_col_pipe_n<N>(a, in, out, status, s);
+
 #define RS_COLBOX_CASE(N) \
   case N: *w = ColPipeGeom<N>::W; *bh = ColPipeGeom<N>::BH; return true;
-#define RS_ROWOK_CASE(N) \
-  case N: return true;
-
-cudaError_t launch_row_pipe_pow3(int n, const RowArgs& a, int* status, cudaStream_t s) {
-  switch (n) {
-    RS_POW3_PIPE_ROW(RS_ROWPIPE_CASE)
-    default: return cudaErrorInvalidValue;
-  }
-}
 
 cudaError_t launch_col_pipe_pow3(int n, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out,
                                  int* status, cudaStream_t s) {
@@ -67,13 +50,6 @@ cudaError_t launch_col_pipe_pow3(int n, const ColArgs& a, const CUtensorMap& in,
 bool col_pipe_box_pow3(int n, int* w, int* bh) {
   switch (n) {
     RS_POW3_PIPE_COL(RS_COLBOX_CASE)
-    default: return false;
-  }
-}
-
-bool row_pipe_ok_pow3(int n) {
-  switch (n) {
-    RS_POW3_PIPE_ROW(RS_ROWOK_CASE)
     default: return false;
   }
 }

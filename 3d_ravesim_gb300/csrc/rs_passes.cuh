@@ -1,5 +1,5 @@
 // rs_passes.cuh — launch templates of the fused row / column passes and of the stage-major
-// twiddle tables. rs_pass_pow2.cu and rs_pass_pow3.cu instantiate them for the two size
+// twiddle tables. rs_pass_pow{2,3}_{rows,cols}.cu instantiate them for the two size
 // families (2^k and 3*2^k) in separate translation units that compile in parallel.
 #pragma once
 #include "rs_pipe.cuh"
@@ -12,8 +12,11 @@ constexpr int rows_per_block() {
   return FftPlan<N>::T >= 256 ? 1 : 256 / FftPlan<N>::T;
 }
 
-template <int N>
-cudaError_t launch_rows_n(const RowArgs& a, cudaStream_t s) {
+#ifndef RS_ROW_VOXMODE
+#define RS_ROW_VOXMODE 1
+#endif
+template <int N, bool VOX>
+cudaError_t launch_rows_nv(const RowArgs& a, cudaStream_t s) {
   constexpr int ROWS = rows_per_block<N>();
   constexpr int THREADS = ROWS * FftPlan<N>::T;
   constexpr size_t SMEM = RowGeom<N, ROWS>::SMEM;
@@ -22,17 +25,26 @@ cudaError_t launch_rows_n(const RowArgs& a, cudaStream_t s) {
   if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
   const unsigned bit = 1u << (dev & 31);
   if (!(configured & bit)) {
-    cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<N, ROWS>,
+    cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<N, ROWS, VOX>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(SMEM));
     if (e != cudaSuccess) return e;
     configured |= bit;
   }
   const int blocks = (a.ny + ROWS - 1) / ROWS;
-  row_pass_kernel<N, ROWS><<<blocks, THREADS, SMEM, s>>>(a);
+  row_pass_kernel<N, ROWS, VOX><<<blocks, THREADS, SMEM, s>>>(a);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) note_launch();
   return e;
+}
+
+// The voxel-transmission specialisation takes the multislice hot path (flags within
+// INV | FWD | TVOX | STORE_U | SCALE, TVOX set); every other combination the general kernel.
+template <int N>
+cudaError_t launch_rows_n(const RowArgs& a, cudaStream_t s) {
+  constexpr int HOT = ROW_INV | ROW_FWD | ROW_TVOX | ROW_STORE_U | ROW_SCALE;
+  if (RS_ROW_VOXMODE && (a.flags & ROW_TVOX) && !(a.flags & ~HOT)) return launch_rows_nv<N, true>(a, s);
+  return launch_rows_nv<N, false>(a, s);
 }
 
 template <int N>
@@ -235,7 +247,7 @@ bool row_pipe_ok_pow3(int n);
 #define RS_POW2_SIZES(X) X(16) X(32) X(64) X(128) X(256) X(512) X(1024) X(2048) X(4096) X(8192) X(16384)
 #define RS_POW3_SIZES(X) X(24) X(48) X(96) X(192) X(384) X(768) X(1536) X(3072) X(6144) X(12288)
 
-// Per-family dispatchers (rs_pass_pow2.cu / rs_pass_pow3.cu); return cudaErrorInvalidValue
+// Per-family dispatchers (rs_pass_pow{2,3}_{rows,cols}.cu); return cudaErrorInvalidValue
 // for a size outside the family.
 cudaError_t launch_row_pass_pow2(int n, const RowArgs& a, cudaStream_t s);
 cudaError_t launch_row_adjoint_pow2(int n, const RowArgs& a, cudaStream_t s);
