@@ -42,7 +42,7 @@ PUBLISHED_MS_PER_LAYER = 43.25
 
 # DRAM bytes per launch of the fused passes at 4096^2 from one ncu capture of this workload
 # (profiles/row_pass_col_pipe_4096.md: dram__bytes.sum.per_second x gpu__time_duration.sum)
-NCU_DRAM_BYTES_4096 = {"row_pass": 221.5e6, "col_pass": 215.5e6}
+NCU_DRAM_BYTES_4096 = {"row_pass": 208.5e6, "col_pass": 215.1e6}
 
 
 def parse():
