@@ -327,6 +327,31 @@ def adjoint_cost(rs, torch, device, n: int = 2048, slices: int = 256) -> dict:
             "checkpoint_every": model.every, "grad_n0_L_Te": [float(t.grad) for t in th]}
 
 
+def plasma_forward_rate(rs, torch, device, n: int = 2048, slices: int = 256, steps: int = 3) -> dict:
+    """Config-3 forward through PlasmaSample.apply: 2048^2, 8 keV, 256 x 2 um slices of a Gaussian
+    plasma (n_e, n_i, T_e, Z* grids of 516^2 float32 per slice, delta/beta evaluated in the row pass)."""
+    wlmod = importlib.import_module("3d_ravesim_gb300.workloads")
+    w = wlmod.gaussian_plasma(n=n, slices=slices)
+    s = w.elements[0]
+    p = w.params
+    u, U = rs.GpuVector.zeros(n * n, device), rs.GpuVector.zeros(n * n, device)
+
+    def run():
+        u.vec.fill_(1.0)
+        s.apply(u, U, p, w.cutoff, 0, None)
+    run()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(steps):
+        run()
+    b.record()
+    b.synchronize()
+    ms = a.elapsed_time(b) / steps
+    return {"case": f"Gaussian plasma {n}^2, {slices} slices, grids {w.info['grid']} float32 x4",
+            "ms_per_run": round(ms, 2), "slice_steps_per_s": round(slices / (ms / 1e3), 1)}
+
+
 def multisim_cost(rs, torch, device, items: int = 128) -> dict:
     """Batched multisim (64 jittered sources x 16 Kramers energies, grid sizes from {1024, 1536,
     2048, 3072}^2, 64-slice shell, 2048^2 area_v1 detector summed incoherently): the first `items`
@@ -477,6 +502,7 @@ def run_ours(args):
         line["plain"] = {"own_fft_unfused": round(plain, 1), "cufft_unfused": round(cufft, 1),
                          "fused_sample_slices": round(fused_rate, 1) if fused_rate else None, "unit": UNIT,
                          "note": "unfused = T kernel, FFT2, H*mask, IFFT2 as separate launches per slice"}
+        line["plasma_forward"] = plasma_forward_rate(rs, torch, device)
         line["adjoint"] = adjoint_cost(rs, torch, device)
         line["multisim"] = multisim_cost(rs, torch, device)
         line["cpu_baseline"] = cpu_baseline(n)
