@@ -21,10 +21,15 @@ namespace rs {
 #else
 #define RS_PACKED 0
 #endif
+#ifndef RS_PACKED_CMUL
+#define RS_PACKED_CMUL 1
+#endif
 #if RS_PACKED
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return __fadd2_rn(a, b); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return __fadd2_rn(a, make_float2(-b.x, -b.y)); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return __fmul2_rn(a, make_float2(s, s)); }
+#endif
+#if RS_PACKED && RS_PACKED_CMUL
 // Complex products as two packed operations: a*b = a.x*(b.x, b.y) + a.y*(-b.y, b.x); each lane is
 // an IEEE multiply then an IEEE fused multiply-add.
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
@@ -35,9 +40,11 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
   return __ffma2_rn(make_float2(a.y, a.y), make_float2(b.y, b.x), __fmul2_rn(make_float2(a.x, a.x), make_float2(b.x, -b.y)));
 }
 #else
+#if !RS_PACKED
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+#endif
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
 }
@@ -53,7 +60,7 @@ __device__ __forceinline__ float2 cmulc(float2 a, float2 b) {
 // (float4 {hi.x, hi.y, lo.x, lo.y}, lo the float nearest to the FP64 rounding residual,
 // hi + lo exact to ~2^-48) and a * w is formed as a*lo + a*hi, the small product first, so
 // that only the final roundings, which depend on a, remain.
-#if RS_PACKED
+#if RS_PACKED && RS_PACKED_CMUL
 __device__ __forceinline__ float2 cmul_tw(float2 a, float4 w) {
   const float2 ax = make_float2(a.x, a.x), ay = make_float2(a.y, a.y);
   const float2 c = __ffma2_rn(ay, make_float2(-w.w, w.z), __fmul2_rn(ax, make_float2(w.z, w.w)));

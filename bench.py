@@ -142,9 +142,13 @@ class Pipeline:
         rs, p, w = self.rs, self.p, self.w
         u, U = self.u, self.U
         z = w.z_first
-        rs.propagation.point_source_propagate_2d(u, U, z - w.source_xyz[2], w.source_xyz[0], w.source_xyz[1], p,
-                                                 w.cutoff)
-        valid = False
+        if w.source_xyz is None:  # unit plane wave at the first element
+            u.vec.fill_(1.0)
+            valid = False
+        else:
+            rs.propagation.point_source_propagate_2d(u, U, z - w.source_xyz[2], w.source_xyz[0], w.source_xyz[1],
+                                                     p, w.cutoff)
+            valid = False
         for el in w.elements:
             if z < el.z_start:
                 rs.propagate_2d(u, U, p.dx, p.get_dy(), p.wl, el.z_start - z, p.chunk_size, w.cutoff, p.nx, p.ny,
@@ -240,15 +244,18 @@ def cpu_baseline(n: int, samples: int = 2) -> dict:
                       f"NumpyVector path, scipy.fft default 1 worker), {dt:.1f} s"}
 
 
-def accuracy_check(rs, torch, device, n: int, slices: int = 4) -> dict:
+def accuracy_check(rs, torch, device, n: int, slices: int = 4, workload: str = "talbot") -> dict:
     """Relative L2 of field and detector intensity vs the FP64 oracle on the benchmark geometry at
     n^2 with `slices` sample slices (a full 512-slice FP64 run at 4096^2 takes hours on the CPU,
-    at 1024^2 about half a minute)."""
+    at 1024^2 about half a minute); workload "shell" is config 0 (plane wave, 1024^2, 128 slices)."""
     from scipy import fft as spfft
 
     from oracle import bigwave_oracle as orc
     wlmod = importlib.import_module("3d_ravesim_gb300.workloads")
-    w = wlmod.talbot_lau(n=n, slices=slices)
+    if workload == "shell":
+        w = wlmod.shell_plane_wave(n=n, slices=slices)
+    else:
+        w = wlmod.talbot_lau(n=n, slices=slices)
     pipe = Pipeline(rs, w, device)
     det = pipe.run()
     torch.cuda.synchronize()
@@ -257,7 +264,10 @@ def accuracy_check(rs, torch, device, n: int, slices: int = 4) -> dict:
     p = w.params
     with spfft.set_workers(os.cpu_count() or 1):
         z = w.z_first
-        u, U = orc.point_source_2d(n, n, p.dx, p.dx, z, 0.0, 0.0, p.wl, w.cutoff)
+        if w.source_xyz is None:
+            u, U = np.ones((n, n), np.complex128), None
+        else:
+            u, U = orc.point_source_2d(n, n, p.dx, p.dx, z, 0.0, 0.0, p.wl, w.cutoff)
         valid = False
         for el in w.elements:
             if z < el.z_start:
@@ -271,7 +281,8 @@ def accuracy_check(rs, torch, device, n: int, slices: int = 4) -> dict:
         u, U = orc.propagate_2d(u, p.dx, p.dx, p.wl, p.z_detector - z, w.cutoff, U=U, skip_fft=True)
     ref_det = orc.detector_area_v1(u, p.dx, p.dx, p.detector_pixel_size_x, p.detector_pixel_size_y,
                                    gpu_det.shape[1], gpu_det.shape[0], p.z_detector)
-    return {"case": f"Talbot-Lau {n}^2 with {slices} sample slices vs FP64 oracle",
+    name = "shell plane wave" if workload == "shell" else "Talbot-Lau"
+    return {"case": f"{name} {n}^2 with {slices} sample slices vs FP64 oracle",
             "field_rel_l2": orc.relative_l2(gpu_u, u),
             "intensity_rel_l2": orc.relative_l2(np.abs(gpu_u) ** 2, np.abs(u) ** 2),
             "detector_rel_l2": orc.relative_l2(gpu_det, ref_det)}
@@ -509,7 +520,8 @@ def run_ours(args):
         # the full slice count at 1024^2 (errors that repeat every slice add up over 514 of them),
         # and the benchmark size itself truncated to 4 sample slices
         line["accuracy"] = [accuracy_check(rs, torch, device, 1024, slices=args.slices),
-                            accuracy_check(rs, torch, device, min(n, 4096))]
+                            accuracy_check(rs, torch, device, min(n, 4096)),
+                            accuracy_check(rs, torch, device, 1024, slices=128, workload="shell")]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
