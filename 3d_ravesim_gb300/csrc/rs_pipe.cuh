@@ -318,10 +318,14 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
   }
   const float4* tw = G::TW_SMEM ? tw_s : tw_g;
   using TWL = typename std::conditional<G::TW_SMEM, TwShared, TwGlobal>::type;
+  // with H applied, the 1/N of the inverse is folded into ey (one product per element fewer)
+  const bool fold = (flags & COL_H) && (flags & COL_SCALE) && !(flags & COL_SPEC);  // U stays unscaled
   if constexpr (G::EY_SMEM) {
     if (flags & COL_H) {  // uniform: a.ey is set whenever H is applied
-      for (int i = threadIdx.x; i < N; i += blockDim.x)
-        ey_s[i] = __ldg(&a.ey[col_exit_pos<N, G::L2>(i % P::T, i / P::T)]);
+      for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const float2 eyv = __ldg(&a.ey[col_exit_pos<N, G::L2>(i % P::T, i / P::T)]);
+        ey_s[i] = fold ? cscale(eyv, a.scale) : eyv;
+      }
     }
     __syncthreads();
   }
@@ -378,7 +382,8 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
         if ((m < 0 ? -m : m) > lim) {
           v[e] = make_float2(0.f, 0.f);
         } else if (flags & COL_H) {
-          const float2 eyv = G::EY_SMEM ? ey_s[e * P::T + t] : __ldg(&a.ey[fy]);
+          const float2 eyv =
+              G::EY_SMEM ? ey_s[e * P::T + t] : (fold ? cscale(__ldg(&a.ey[fy]), a.scale) : __ldg(&a.ey[fy]));
           v[e] = cmul(v[e], cmul(exv, eyv));
         }
       }
@@ -388,7 +393,7 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
 #pragma unroll
       for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(col_exit_pos<N, G::L2>(t, e)) * nx + x] = v[e];
     }
-    if (flags & COL_SCALE) {
+    if ((flags & COL_SCALE) && !fold) {
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = cscale(v[e], a.scale);
     }
