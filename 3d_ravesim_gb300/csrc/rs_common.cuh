@@ -7,6 +7,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
 namespace rs {
 
 // Blackwell (sm_100+) executes two FP32 adds / multiplies of a register pair in one
@@ -211,12 +213,78 @@ __device__ __forceinline__ void dft3(float2& a0, float2& a1, float2& a2) {
   a2 = csub(m, q);
 }
 
+// cos(pi/12), sin(pi/12) (15 degrees) as float + residual, for the radix-24 inner twiddles.
+constexpr float kC12 = 0.96592582628906828675f;
+constexpr float kS12 = 0.25881904510252076235f;
+constexpr float kC12lo = 1.3567816203874372e-08f;
+constexpr float kS12lo = 1.4661987179920288e-09f;
+
+// Multiply by W24^M = exp(-+2*pi*i*M/24) for the M used inside the 3 x 8 radix-24 butterfly.
+template <int M, bool INV>
+__device__ __forceinline__ float2 tw24(float2 a) {
+  if constexpr (M == 0) {
+    return a;
+  } else if constexpr (M == 3) {
+    return tw16<2, INV>(a);  // 45 degrees
+  } else if constexpr (M == 6) {
+    return mul_mi<INV>(a);
+  } else if constexpr (M == 12) {
+    return make_float2(-a.x, -a.y);
+  } else {
+    // forward exp(-i*15deg*M) = (wr, wi0), residuals (wrl, wil0); the halves are exact
+    constexpr float wr = M == 1 ? kC12 : M == 2 ? kHalfSqrt3 : M == 4 ? 0.5f : M == 5 ? kS12 : M == 7 ? -kS12
+                       : M == 8 ? -0.5f : -kHalfSqrt3;                                  // M = 10, 14
+    constexpr float wi0 = M == 1 ? -kS12 : M == 2 ? -0.5f : M == 4 ? -kHalfSqrt3 : M == 5 ? -kC12
+                        : M == 7 ? -kC12 : M == 8 ? -kHalfSqrt3 : M == 10 ? -0.5f : 0.5f;  // M = 14
+    constexpr float wrl = M == 1 ? kC12lo : M == 2 ? kHalfSqrt3lo : M == 5 ? kS12lo : M == 7 ? -kS12lo
+                        : (M == 10 || M == 14) ? -kHalfSqrt3lo : 0.0f;
+    constexpr float wil0 = M == 1 ? -kS12lo : (M == 4 || M == 8) ? -kHalfSqrt3lo : (M == 5 || M == 7) ? -kC12lo
+                         : 0.0f;
+    static_assert(M == 1 || M == 2 || M == 4 || M == 5 || M == 7 || M == 8 || M == 10 || M == 14, "W24 power");
+    return cmul_tw(a, make_float4(wr, INV ? -wi0 : wi0, wrl, INV ? -wil0 : wil0));
+  }
+}
+
+// 24-point DFT as 3 x 8: index n = 8 n1 + n2, k = k1 + 3 k2; 3-point DFTs over n1, inner
+// twiddles W24^(n2 k1), 8-point DFTs over n2, transpose. Natural order in and out.
+template <int K1, bool INV, int... N2>
+__device__ __forceinline__ void tw24_row(float2 (&a)[24], std::integer_sequence<int, N2...>) {
+  ((a[8 * K1 + N2] = tw24<N2 * K1, INV>(a[8 * K1 + N2])), ...);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft24(float2 (&a)[24]) {
+#pragma unroll
+  for (int n2 = 0; n2 < 8; ++n2) dft3<INV>(a[n2], a[8 + n2], a[16 + n2]);
+  tw24_row<1, INV>(a, std::make_integer_sequence<int, 8>{});
+  tw24_row<2, INV>(a, std::make_integer_sequence<int, 8>{});
+#pragma unroll
+  for (int k1 = 0; k1 < 3; ++k1) {
+    float2 b[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i] = a[8 * k1 + i];
+    dft8<INV>(b);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[8 * k1 + i] = b[i];
+  }
+  float2 y[24];
+#pragma unroll
+  for (int k1 = 0; k1 < 3; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 8; ++k2) y[k1 + 3 * k2] = a[8 * k1 + k2];
+#pragma unroll
+  for (int k = 0; k < 24; ++k) a[k] = y[k];
+}
+
 // Radix-R DFT on the R registers v[OFF .. OFF+R-1] of an E-register array.
 template <int R, bool INV, int OFF, int E>
 __device__ __forceinline__ void dft_slice(float2 (&v)[E]) {
   if constexpr (R == 16) {
     static_assert(E == 16 && OFF == 0, "radix-16 stages use the whole 16-register array");
     dft16<INV>(v);
+  } else if constexpr (R == 24) {
+    static_assert(E == 24 && OFF == 0, "radix-24 stages use the whole 24-register array");
+    dft24<INV>(v);
   } else if constexpr (R == 8) {
     float2 a[8];
 #pragma unroll

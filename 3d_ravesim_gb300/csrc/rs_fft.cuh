@@ -29,7 +29,8 @@ __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c
 template <int N>
 struct FftPlan {
   // Power-of-two lengths: 16 values per thread, radix-16 stages plus one radix-2/4/8 stage.
-  // Lengths 3*2^k: 24 values per thread, radix-8 stages, one radix-2/4 stage, one radix-3 stage.
+  // Lengths 3*2^k: 24 values per thread, a radix-24 stage (3 x 8 in registers), radix-8
+  // stages and one radix-2/4 stage (one exchange fewer than a separate radix-3 stage).
   static constexpr bool POW2 = (N & (N - 1)) == 0;
   static constexpr int M = POW2 ? N : N / 3;
   static_assert((M & (M - 1)) == 0 && (POW2 || M * 3 == N), "N must be 2^k or 3*2^k");
@@ -39,12 +40,12 @@ struct FftPlan {
   static constexpr int LB = POW2 ? 4 : 3;
   static constexpr int NBIG = LG / LB;
   static constexpr int REM = 1 << (LG % LB);
-  static constexpr int NST = NBIG + (REM > 1 ? 1 : 0) + (POW2 ? 0 : 1);
+  static constexpr int NST = NBIG + (REM > 1 ? 1 : 0);
   static constexpr int E = POW2 ? 16 : 24;       // values per thread
   static constexpr int T = N / E;                // threads per sequence
   static constexpr int S = N + N / 16;           // padded shared buffer length
   __host__ __device__ static constexpr int fwd_radix(int s) {
-    return s < NBIG ? BIG : ((s == NBIG && REM > 1) ? REM : 3);
+    return s < NBIG ? ((!POW2 && s == 0) ? 24 : BIG) : REM;
   }
   __host__ __device__ static constexpr int radix(bool inv, int s) { return fwd_radix(inv ? (NST - 1 - s) : s); }
   __host__ __device__ static constexpr int entry_radix(bool inv) { return radix(inv, 0); }

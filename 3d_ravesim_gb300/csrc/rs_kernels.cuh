@@ -342,8 +342,11 @@ __device__ __forceinline__ float2 point_source_value(const PointSrcArgs& p, int 
 // blocks per SM the row pass's registers are sized for (one 256-thread row block: 4 -> <= 64
 // registers; the few spilled values cost less than the warps a fourth block adds)
 template <int N, int ROWS>
+#ifndef RS_ROW_MINB_POW3
+#define RS_ROW_MINB_POW3 3
+#endif
 constexpr int row_minb() {
-  return ROWS * FftPlan<N>::T <= 256 ? (FftPlan<N>::E == 16 ? RS_ROW_MINB : 2) : 1;
+  return ROWS * FftPlan<N>::T <= 256 ? (FftPlan<N>::E == 16 ? RS_ROW_MINB : RS_ROW_MINB_POW3) : 1;
 }
 
 // Shared memory of a row block: the exchange buffers (S per row), then a voxel-row prefetch
