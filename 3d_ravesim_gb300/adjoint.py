@@ -10,8 +10,10 @@ Adjoint (Wirtinger calculus, g = dL/dconj(u)):
   transmission  dL/dconj(t) = conj(u) * v,  g = conj(t) * v            (rs_adjoint_slice)
                 dL/ddelta = 4 pi t/wl Im(conj(conj(u) v) t), dL/dbeta = -4 pi t/wl Re(...)
 scattered to the voxels through the bilinear weights. Slice fields are checkpointed every
-`checkpoint_every` slices and recomputed segment by segment on the way back (every slice is
-kept when checkpoint_every is 1).
+`checkpoint_every` slices (default ~sqrt(nz)) and recomputed segment by segment on the way back;
+checkpoint_every=0 instead keeps the field entering every slice (written by the forward row
+pass itself), so the backward needs no recomputation: nz fields of nx*ny*8 bytes, 8.6 GB for
+256 slices at 2048^2, which a GB300's HBM holds easily.
 """
 from __future__ import annotations
 
@@ -54,6 +56,7 @@ class MultisliceModel:
         self.u_final = None
         self.last_backward = None  # "fused" (two passes per slice) or "per-slice"
         self.fused = True          # False forces the per-slice backward
+        self.fields: torch.Tensor | None = None  # checkpoint_every == 0: every slice's entering field
 
     # -- helpers ------------------------------------------------------------------------------
     def _vgeom(self, db: torch.Tensor) -> _lib.VoxelGeom:
@@ -82,13 +85,19 @@ class MultisliceModel:
         if db.dtype != torch.float32 or db.dim() != 4 or db.shape[3] != 2 or not db.is_contiguous():
             raise ValueError("db must be a contiguous (nz, ny_v, nx_v, 2) float32 tensor")
         nz = db.shape[0]
-        every = self.checkpoint_every or max(1, int(round(math.sqrt(nz))))
-        self.every = every
         self.u.vec.copy_(self.u0.reshape(-1))
         self.checkpoints = {}
-        for s0 in range(0, nz, every):
-            self.checkpoints[s0] = self.u.vec.clone()
-            self._step_slices(db, s0, min(nz, s0 + every))
+        self.fields = None
+        start = self.u.vec.clone()
+        if self.checkpoint_every == 0 and self.fused and self._forward_store_all(db):
+            self.every = nz
+            self.checkpoints[0] = start  # lets the per-slice backward recompute if it is forced
+        else:
+            every = self.checkpoint_every or max(1, int(round(math.sqrt(nz))))
+            self.every = every
+            for s0 in range(0, nz, every):
+                self.checkpoints[s0] = self.u.vec.clone()
+                self._step_slices(db, s0, min(nz, s0 + every))
         p = self.p
         propagate_2d(self.u, self.U, p.dx, p.get_dy(), p.wl, self._final_dz(nz), p.chunk_size, self.cutoff,
                      p.nx, p.ny, skip_fft=True)
@@ -140,6 +149,22 @@ class MultisliceModel:
         return grad
 
 
+    def _forward_store_all(self, db: torch.Tensor) -> bool:
+        """The whole forward in one fused call that also keeps every slice's entering field;
+        False (nothing run) when the size is not supported by the fused adjoint."""
+        p = self.p
+        nz = db.shape[0]
+        plan = _lib.plan_for(p.nx, p.ny, self.device)
+        if not plan.fast or p.nx & (p.nx - 1) or 3 * db.shape[2] > p.nx + p.nx // 16:
+            return False
+        self.fields = torch.empty((nz, p.nx * p.ny), dtype=torch.complex64, device=self.device)
+        with torch.cuda.device(self.device):
+            _lib.check(_lib.lib().rs_multislice_dbgrid_store(
+                plan.handle, _lib.ptr(self.u.vec), _lib.ptr(self.U.vec), _lib.ptr(db), self._vgeom(db),
+                float(p.dx), float(p.get_dy()), float(p.wl), self.cutoff, _lib.doubles(self._dz(nz)), None, 0, nz,
+                _lib.ptr(self.fields), _lib.stream_handle()), "rs_multislice_dbgrid_store")
+        return True
+
     def _backward_fused(self, db, g, grad, vg, plan, st) -> bool:
         """Backward sweep in two fused passes per slice (rs_adjoint_multislice_dbgrid), each segment's
         fields recomputed from its checkpoint by rs_multislice_dbgrid_store. False when the size is
@@ -149,6 +174,13 @@ class MultisliceModel:
         nz = db.shape[0]
         n = p.nx * p.ny
         dz = _lib.doubles(self._dz(nz))
+        if self.fields is not None:  # every field kept by the forward: one sweep, nothing recomputed
+            with torch.cuda.device(self.device):
+                _lib.check(lib.rs_adjoint_multislice_dbgrid(plan.handle, _lib.ptr(g.vec), _lib.ptr(db), vg,
+                                                            float(p.dx), float(p.get_dy()), float(p.wl), self.cutoff,
+                                                            dz, None, 0, nz, _lib.ptr(self.fields), _lib.ptr(grad),
+                                                            st), "rs_adjoint_multislice_dbgrid")
+            return True
         fields = torch.empty((self.every, n), dtype=torch.complex64, device=self.device)
         for s0 in sorted(self.checkpoints, reverse=True):
             s1 = min(nz, s0 + self.every)

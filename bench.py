@@ -288,7 +288,7 @@ def accuracy_check(rs, torch, device, n: int, slices: int = 4, workload: str = "
             "detector_rel_l2": orc.relative_l2(gpu_det, ref_det)}
 
 
-def adjoint_cost(rs, torch, device, n: int = 2048, slices: int = 256) -> dict:
+def adjoint_cost(rs, torch, device, n: int = 2048, slices: int = 256, checkpoint_every=None) -> dict:
     """Gradient cost of the differentiable plasma workload (2048^2, 8 keV, 256 x 2 um slices of a
     Gaussian plasma, n0 = 1e21 cm^-3, L = 150 um, T_e = 500 eV): one forward pass against one
     forward + adjoint (loss L2, gradients to every voxel's delta/beta and to n0, L, T_e)."""
@@ -301,7 +301,7 @@ def adjoint_cost(rs, torch, device, n: int = 2048, slices: int = 256) -> dict:
     p = rs.SimParams(N=n * n, nx=n, ny=n, dx=dx, dy=dx, z_detector=0.1 + slices * pz + 0.2, detector_size=n * dx,
                      detector_pixel_size_x=dx, detector_pixel_size_y=dx, wl=wl, chunk_size=n)
     u0 = torch.ones(n * n, dtype=torch.complex64, device=device)
-    model = adj.MultisliceModel(p, geom, 0.45 / dx, u0)
+    model = adj.MultisliceModel(p, geom, 0.45 / dx, u0, checkpoint_every=checkpoint_every)
     th = [torch.tensor(v, dtype=torch.float64, device=device, requires_grad=True) for v in (1e21, 150e-6, 500.0)]
 
     def fwd(params=th):
@@ -335,7 +335,8 @@ def adjoint_cost(rs, torch, device, n: int = 2048, slices: int = 256) -> dict:
             "Poisson-noisy (1e4 photons/pixel) image of n0 = 1.05e21, L = 145 um, T_e = 550 eV",
             "backward": model.last_backward, "forward_ms": round(f_ms, 2),
             "forward_plus_gradient_ms": round(g_ms, 2), "ratio": round(g_ms / f_ms, 2),
-            "checkpoint_every": model.every, "grad_n0_L_Te": [float(t.grad) for t in th]}
+            "checkpoint_every": model.every if checkpoint_every != 0 else "every field kept",
+            "grad_n0_L_Te": [float(t.grad) for t in th]}
 
 
 def plasma_forward_rate(rs, torch, device, n: int = 2048, slices: int = 256, steps: int = 3) -> dict:
@@ -514,7 +515,7 @@ def run_ours(args):
                          "fused_sample_slices": round(fused_rate, 1) if fused_rate else None, "unit": UNIT,
                          "note": "unfused = T kernel, FFT2, H*mask, IFFT2 as separate launches per slice"}
         line["plasma_forward"] = plasma_forward_rate(rs, torch, device)
-        line["adjoint"] = adjoint_cost(rs, torch, device)
+        line["adjoint"] = [adjoint_cost(rs, torch, device), adjoint_cost(rs, torch, device, checkpoint_every=0)]
         line["multisim"] = multisim_cost(rs, torch, device)
         line["cpu_baseline"] = cpu_baseline(n)
         # the full slice count at 1024^2 (errors that repeat every slice add up over 514 of them),

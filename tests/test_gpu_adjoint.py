@@ -45,7 +45,7 @@ def oracle_loss(oracle, db, p, geom, cutoff, target):
 
 
 @pytest.mark.parametrize("every,pitch,path", [(None, 0.85e-6, "per-slice"), (1, 0.85e-6, "per-slice"),
-                                              (None, 2e-6, "fused"), (3, 2e-6, "fused")])
+                                              (None, 2e-6, "fused"), (3, 2e-6, "fused"), (0, 2e-6, "fused")])
 def test_adjoint_matches_fp64_finite_differences(rs, cuda, oracle, every, pitch, path):
     adj, model, db, p, geom = setup_case(rs, cuda, n=128 if path == "fused" else 64, nz=5, every=every, pitch=pitch)
     dbt = torch.from_numpy(db).to(cuda)
