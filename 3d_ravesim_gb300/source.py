@@ -3,6 +3,8 @@ from __future__ import annotations
 
 from dataclasses import dataclass
 
+import numpy as np
+
 from .propagation import SimParams, fresnel_plane_propagate_2d, grid_density_check_2d, point_source_propagate_2d
 
 
@@ -30,8 +32,11 @@ class PointSource:
                 raise ValueError("physical-z source history is not supported with Fresnel scaling")
             fresnel_plane_propagate_2d(u, U, dz, self.x, self.y, sim_params, cutoff_freq)
             return
-        if history is not None:
-            raise NotImplementedError("analytic source history is not part of this build")
         grid_density_check_2d(dz, self.x, sim_params.nx, sim_params.dx, self.y, sim_params.ny,
                               sim_params.get_dy(), sim_params.wl)
         point_source_propagate_2d(u, U, dz, self.x, self.y, sim_params, cutoff_freq)
+        if history is not None:
+            # analytic frames at z = k * history dz below z_out (big-wave/source.py:109-113)
+            from .history import generate_analytic_history_2d
+            zs = np.arange(0, z_out, history[1])[1:]
+            generate_analytic_history_2d(history[0], zs, self.x, self.y, sim_params, cutoff_freq)
