@@ -72,6 +72,9 @@ _SIGS = {
                           _P, _P], c_int),
     "rs_detector_adjoint": ([_P, _P, _P, _P, ctypes.POINTER(DetectorGeom), _P], c_int),
     "rs_plan_set_pipeline": ([_P, c_int], c_int),
+    "rs_plan_set_schedule": ([_P, c_int], c_int),
+    "rs_plan_get_schedule": ([_P, ctypes.POINTER(c_int)], c_int),
+    "rs_plan_schedules": ([_P, ctypes.POINTER(c_int), c_int, ctypes.POINTER(c_int)], c_int),
     "rs_plan_status": ([_P, ctypes.POINTER(c_int)], c_int),
     "rs_detector_noalloc": ([_P, c_int, c_int, _P, ctypes.POINTER(DetectorGeom), _P], c_int),
     "rs_launch_count": ([ctypes.POINTER(ctypes.c_ulonglong)], c_int),
@@ -154,6 +157,23 @@ class Plan:
         with torch.cuda.device(self.device):
             check(lib().rs_plan_set_pipeline(self.handle, mask), "rs_plan_set_pipeline")
 
+    def set_schedule(self, mask: int) -> None:
+        """Pass schedule bits: 1 pipelined rows, 2 pipelined columns, 4 general row kernel."""
+        with torch.cuda.device(self.device):
+            check(lib().rs_plan_set_schedule(self.handle, int(mask)), "rs_plan_set_schedule")
+
+    def schedule(self) -> int:
+        m = c_int(0)
+        check(lib().rs_plan_get_schedule(self.handle, ctypes.byref(m)), "rs_plan_get_schedule")
+        return m.value
+
+    def schedules(self) -> list[int]:
+        """The schedule masks that are distinct for this plan's sizes."""
+        buf = (c_int * 8)()
+        n = c_int(0)
+        check(lib().rs_plan_schedules(self.handle, buf, 8, ctypes.byref(n)), "rs_plan_schedules")
+        return [buf[i] for i in range(min(n.value, 8))]
+
     def status(self) -> int:
         """Synchronise and return the device status word (0 = no bounded wait gave up)."""
         st = c_int(0)
@@ -195,6 +215,8 @@ def plan_for(nx: int, ny: int, device: torch.device, slot: int | None = None) ->
     if p is None:
         p = Plan(nx, ny, torch.device("cuda", idx))
         _plans[key] = p
+        from . import autotune
+        autotune.apply_to_plan(p)  # the cached pass schedule of this device and size, if any
     return p
 
 

@@ -96,9 +96,12 @@ struct rs_plan {
     rs_detector_geom g{};
     size_t off[8] = {};
   } det_cache;
-  // pipelined (bulk-copy) passes per direction; RS_PIPELINE / rs_plan_set_pipeline select them
+  // Pass schedule (rs_plan_set_schedule): pipelined (bulk-copy, persistent) passes per direction,
+  // and whether the voxel-only row kernel takes the multislice rows. RS_PIPELINE sets the first two
+  // at plan creation.
   bool pipe_rows = true;
   bool pipe_cols = true;
+  bool row_vox = true;
   int* status = nullptr;  // device word set by bounded waits that gave up
   struct MapEntry {
     const void* ptr = nullptr;
@@ -202,7 +205,7 @@ cudaError_t run_row(rs_plan* p, const RowArgs& r, cudaStream_t s) {
   if (p->pipe_rows && !(r.flags & ROW_STORE_U) && row_pipe_ok(p->nx) && (r.flags & ROW_SRC || aligned16(r.in)) &&
       aligned16(r.out))
     return launch_row_pipe(p->nx, r, p->status, s);
-  return launch_row_pass(p->nx, r, s);
+  return launch_row_pass(p->nx, r, s, p->row_vox);
 }
 
 cudaError_t run_col(rs_plan* p, const ColArgs& ca, cudaStream_t s) {
@@ -588,8 +591,46 @@ int rs_plan_is_fast(const rs_plan* p) { return p && p->fast ? 1 : 0; }
 
 int rs_plan_set_pipeline(rs_plan* p, int mask) {
   RS_TRY(check_plan(p));
-  p->pipe_rows = (mask & 1) != 0;
-  p->pipe_cols = (mask & 2) != 0;
+  p->pipe_rows = (mask & RS_SCHED_PIPE_ROWS) != 0;
+  p->pipe_cols = (mask & RS_SCHED_PIPE_COLS) != 0;
+  return RS_OK;
+}
+
+int rs_plan_set_schedule(rs_plan* p, int mask) {
+  RS_TRY(check_plan(p));
+  if (mask & ~(RS_SCHED_PIPE_ROWS | RS_SCHED_PIPE_COLS | RS_SCHED_ROW_GENERAL))
+    return fail(RS_EINVAL, "unknown schedule bits 0x%x", mask);
+  p->pipe_rows = (mask & RS_SCHED_PIPE_ROWS) != 0;
+  p->pipe_cols = (mask & RS_SCHED_PIPE_COLS) != 0;
+  p->row_vox = (mask & RS_SCHED_ROW_GENERAL) == 0;
+  return RS_OK;
+}
+
+int rs_plan_get_schedule(const rs_plan* p, int* mask) {
+  RS_TRY(check_plan(p));
+  if (!mask) return fail(RS_EINVAL, "mask is NULL");
+  *mask = (p->pipe_rows ? RS_SCHED_PIPE_ROWS : 0) | (p->pipe_cols ? RS_SCHED_PIPE_COLS : 0) |
+          (p->row_vox ? 0 : RS_SCHED_ROW_GENERAL);
+  return RS_OK;
+}
+
+int rs_plan_schedules(const rs_plan* p, int* masks, int cap, int* count) {
+  RS_TRY(check_plan(p));
+  if (!count || (cap > 0 && !masks)) return fail(RS_EINVAL, "count/masks is NULL");
+  // Distinct pass schedules for this plan's sizes: a bit whose variant does not exist for the
+  // size (no pipelined kernel, or the direct-DFT path of a generic size) would change nothing.
+  int w = 0, bh = 0;
+  const bool rows_pipe = p->fast && row_pipe_ok(p->nx);
+  const bool cols_pipe = p->fast && col_pipe_box(p->ny, &w, &bh);
+  int n = 0;
+  for (int m = 0; m < 8; ++m) {
+    if ((m & RS_SCHED_PIPE_ROWS) && !rows_pipe) continue;
+    if ((m & RS_SCHED_PIPE_COLS) && !cols_pipe) continue;
+    if ((m & RS_SCHED_ROW_GENERAL) && (!p->fast || (m & RS_SCHED_PIPE_ROWS))) continue;
+    if (n < cap) masks[n] = m;
+    ++n;
+  }
+  *count = n;
   return RS_OK;
 }
 

@@ -11,8 +11,8 @@ bool fast_size(int n) {
   return n % 3 == 0 && is_pow2(n / 3) && n >= 24 && n <= 12288;
 }
 
-cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s) {
-  return is_pow2(nx) ? launch_row_pass_pow2(nx, a, s) : launch_row_pass_pow3(nx, a, s);
+cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s, bool vox) {
+  return is_pow2(nx) ? launch_row_pass_pow2(nx, a, vox, s) : launch_row_pass_pow3(nx, a, vox, s);
 }
 
 cudaError_t launch_row_adjoint(int nx, const RowArgs& a, cudaStream_t s) {

@@ -679,7 +679,8 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T, (W * FftPlan<N>::T <= 512 ?
 // Counts kernel launches made by this library (read through rs_launch_count).
 void note_launch(unsigned n = 1);
 
-cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s);
+// vox = false keeps the voxel-transmission specialisation out (a schedule choice of the plan).
+cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s, bool vox = true);
 // Adjoint row pass (row_adjoint_kernel) for power-of-two nx; cudaErrorInvalidValue otherwise.
 cudaError_t launch_row_adjoint(int nx, const RowArgs& a, cudaStream_t s);
 // Compensated stage-major twiddle tables of the fused passes for length n (fast sizes only).

@@ -4,9 +4,9 @@
 namespace rs {
 
 #define RS_ROW_CASE(N) \
-  case N: return launch_rows_n<N>(a, s);
+  case N: return launch_rows_n<N>(a, vox, s);
 
-cudaError_t launch_row_pass_pow3(int n, const RowArgs& a, cudaStream_t s) {
+cudaError_t launch_row_pass_pow3(int n, const RowArgs& a, bool vox, cudaStream_t s) {
   switch (n) {
     RS_POW3_SIZES(RS_ROW_CASE)
     default: return cudaErrorInvalidValue;

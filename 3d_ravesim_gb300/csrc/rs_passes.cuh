@@ -39,11 +39,12 @@ cudaError_t launch_rows_nv(const RowArgs& a, cudaStream_t s) {
 }
 
 // The voxel-transmission specialisation takes the multislice hot path (flags within
-// INV | FWD | TVOX | STORE_U | SCALE, TVOX set); every other combination the general kernel.
+// INV | FWD | TVOX | STORE_U | SCALE, TVOX set) unless the caller's schedule turns it off
+// (vox = false); every other combination runs the general kernel.
 template <int N>
-cudaError_t launch_rows_n(const RowArgs& a, cudaStream_t s) {
+cudaError_t launch_rows_n(const RowArgs& a, bool vox, cudaStream_t s) {
   constexpr int HOT = ROW_INV | ROW_FWD | ROW_TVOX | ROW_STORE_U | ROW_SCALE;
-  if (RS_ROW_VOXMODE && (a.flags & ROW_TVOX) && !(a.flags & ~HOT)) return launch_rows_nv<N, true>(a, s);
+  if (RS_ROW_VOXMODE && vox && (a.flags & ROW_TVOX) && !(a.flags & ~HOT)) return launch_rows_nv<N, true>(a, s);
   return launch_rows_nv<N, false>(a, s);
 }
 
@@ -249,9 +250,9 @@ bool row_pipe_ok_pow3(int n);
 
 // Per-family dispatchers (rs_pass_pow{2,3}_{rows,cols}.cu); return cudaErrorInvalidValue
 // for a size outside the family.
-cudaError_t launch_row_pass_pow2(int n, const RowArgs& a, cudaStream_t s);
+cudaError_t launch_row_pass_pow2(int n, const RowArgs& a, bool vox, cudaStream_t s);
 cudaError_t launch_row_adjoint_pow2(int n, const RowArgs& a, cudaStream_t s);
-cudaError_t launch_row_pass_pow3(int n, const RowArgs& a, cudaStream_t s);
+cudaError_t launch_row_pass_pow3(int n, const RowArgs& a, bool vox, cudaStream_t s);
 cudaError_t launch_col_pass_pow2(int n, const ColArgs& a, cudaStream_t s);
 cudaError_t launch_col_pass_pow3(int n, const ColArgs& a, cudaStream_t s);
 cudaError_t launch_stage_twiddles_pow2(int n, float4* tw, cudaStream_t s);

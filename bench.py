@@ -165,6 +165,14 @@ def l2_flush_buffer(torch, device):
     return torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
 
 
+def schedule_name(mask: int) -> str:
+    """Readable form of a pass-schedule mask (bits: 1 pipelined rows, 2 pipelined columns,
+    4 general row kernel)."""
+    rows = "rows:pipelined" if mask & 1 else ("rows:per-block" if mask & 4 else "rows:per-block-voxel")
+    cols = "cols:pipelined" if mask & 2 else "cols:per-block"
+    return f"{rows},{cols}"
+
+
 def time_steps(torch, fn, steps, flush, stream):
     """Sum of per-step CUDA-event times; the L2 flush between steps is outside the events."""
     total = 0.0
@@ -383,11 +391,26 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
         runner.run(**kw)
         torch.cuda.synchronize()
         out[name + "_s"] = round(time.perf_counter() - t0, 3)
+    # the same batch captured as one CUDA graph (items on 2 streams, the detector sum inside),
+    # launched once per batch
+    graphed = ms.BatchRunner(b, device, streams=2)
+    t0 = time.perf_counter()
+    graphed.capture()
+    capture_s = time.perf_counter() - t0
+    graphed.replay()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    graphed.replay()
+    out["fused_graph_s"] = round(time.perf_counter() - t0, 3)
+    del graphed
     slices = b.sample.grid.shape[0]
-    return {"case": f"{items} of 1024 items, sizes {b.info['sizes']}, {slices} slices each",
-            "fused_items_per_s": round(items / out["fused_s"], 2),
-            "plain_loop_items_per_s": round(items / out["plain_loop_s"], 2),
-            "speedup": round(out["plain_loop_s"] / out["fused_s"], 2), **out}
+    res = {"case": f"{items} of 1024 items, sizes {b.info['sizes']}, {slices} slices each",
+           "fused_items_per_s": round(items / out["fused_s"], 2),
+           "fused_graph_items_per_s": round(items / out["fused_graph_s"], 2),
+           "plain_loop_items_per_s": round(items / out["plain_loop_s"], 2),
+           "speedup": round(out["plain_loop_s"] / min(out["fused_s"], out["fused_graph_s"]), 2),
+           "graph_capture_s": round(capture_s, 2), **out}
+    return res
 
 
 def run_ours(args):
@@ -410,6 +433,11 @@ def run_ours(args):
     else:
         w = wlmod.talbot_lau(n=args.n, slices=args.slices)
     pipe = Pipeline(rs, w, device)
+    # pass schedule of the field's plan: every distinct schedule timed on a few seeded voxel
+    # slices of this size, the fastest kept (nothing is read from or written to the cache file)
+    autotune = importlib.import_module("3d_ravesim_gb300.autotune")
+    tuned = autotune.tune_multislice(w.params.nx, w.params.ny, device, store=False)
+    rs._lib.plan_for(w.params.nx, w.params.ny, device).set_schedule(tuned.mask)
     stream = torch.cuda.current_stream(device)
     flush = l2_flush_buffer(torch, device)
     det = torch.zeros((int(w.params.get_detector_size_y() // w.params.detector_pixel_size_y),
@@ -487,7 +515,12 @@ def run_ours(args):
                        "sample_slices": args.slices, "voxel_grid": vox, "energy_ev": w.info["energy_ev"],
                        "l2": "256 MiB buffer written between timed steps (flush outside the events)",
                        "parallelism": f"replicas x{world} (one field per GPU)"},
-            "roofline": roofline, "gpu_launches": launches, "clocks": clocks.summary()}
+            "roofline": roofline, "gpu_launches": launches, "clocks": clocks.summary(),
+            "schedule": {"mask": tuned.mask, "passes": schedule_name(tuned.mask),
+                         "tuned_ms_per_schedule": {schedule_name(m): round(t, 3)
+                                                   for m, t in sorted(tuned.timings_ms.items())},
+                         "tuned_on": f"{tuned.slices} seeded voxel slices at {n}^2",
+                         "max_rel_diff_between_schedules": max(tuned.rel_diff.values())}}
 
     if rank == 0 and not args.no_extras:
         # e2e: every step copies its voxel grids in from pinned host memory and the detector image

@@ -206,6 +206,22 @@ int rs_detector(rs_plan* plan, const void* u, double* out, const rs_detector_geo
  * them for the row passes, bit 1 for the column passes (default: columns only). RS_PIPELINE in
  * the environment ("0", "1", "rows", "cols") overrides the default at plan creation. */
 int rs_plan_set_pipeline(rs_plan* plan, int mask);
+
+/* Pass schedule of a plan (the autotuner's choices; every variant computes the same transform):
+ *   RS_SCHED_PIPE_ROWS   row passes as the persistent bulk-copy pipeline (tiles of rows staged
+ *                        through shared memory by a producer warp);
+ *   RS_SCHED_PIPE_COLS   column passes as the persistent tensor-copy pipeline (strips of columns
+ *                        loaded by TMA boxes, NB buffers) instead of one block per strip;
+ *   RS_SCHED_ROW_GENERAL the multislice rows run the general row kernel instead of the
+ *                        voxel-only specialisation.
+ * rs_plan_schedules lists the masks that are distinct for the plan's sizes (it writes at most
+ * `cap` of them and the total to *count). No reference function: big-wave has one FFT schedule. */
+#define RS_SCHED_PIPE_ROWS 1
+#define RS_SCHED_PIPE_COLS 2
+#define RS_SCHED_ROW_GENERAL 4
+int rs_plan_set_schedule(rs_plan* plan, int mask);
+int rs_plan_get_schedule(const rs_plan* plan, int* mask);
+int rs_plan_schedules(const rs_plan* plan, int* masks, int cap, int* count);
 /* Synchronises the device and returns the plan's device status word: 0, or non-zero (with
  * RS_ETIMEOUT) if a pipelined pass gave up waiting for a bulk copy. */
 int rs_plan_status(rs_plan* plan, int* device_status);

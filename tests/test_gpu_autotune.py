@@ -1,0 +1,54 @@
+"""Schedule autotuner on the GPU: the distinct schedules of a size, every schedule reproducing
+the first one's multislice field, the cached choice taken by plans created afterwards."""
+import importlib
+
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture()
+def at(monkeypatch, tmp_path):
+    monkeypatch.setenv("RS_SCHEDULE_CACHE", str(tmp_path / "schedules.json"))
+    monkeypatch.delenv("RS_AUTOTUNE", raising=False)
+    return importlib.import_module("3d_ravesim_gb300.autotune")
+
+
+def test_schedule_lists(rs, cuda):
+    lib = rs._lib
+    assert lib.plan_for(4096, 4096, cuda).schedules() == [0, 1, 2, 3, 4, 6]
+    assert lib.plan_for(8192, 64, cuda).schedules() == [0, 1, 4]
+    assert lib.plan_for(72, 40, cuda).schedules() == [0]  # direct-DFT sizes have one schedule
+    p = lib.plan_for(1024, 1024, cuda)
+    old = p.schedule()
+    p.set_schedule(6)
+    assert p.schedule() == 6
+    p.set_schedule(old)
+    with pytest.raises(Exception):
+        p.set_schedule(8)
+
+
+@pytest.mark.parametrize("n", [1024, 1536])
+def test_tune_multislice(rs, cuda, at, n):
+    c = at.tune_multislice(n, n, cuda, reps=3)
+    plan = rs._lib.plan_for(n, n, cuda)
+    assert sorted(c.timings_ms) == plan.schedules()
+    assert all(t > 0 for t in c.timings_ms.values())
+    # the pipelined and per-block kernels compute the same values (the rounding of each step is
+    # spelled out), so every schedule reproduces the first one's field
+    assert max(c.rel_diff.values()) <= at.MAX_SCHEDULE_DIFF, c.rel_diff
+    assert c.mask in plan.schedules()
+    assert at.cached_schedule(n, n, cuda) == c.mask
+    # a plan created afterwards (another slot) takes the cached schedule
+    with rs._lib.plan_slot(7):
+        fresh = rs._lib.plan_for(n, n, cuda)
+    assert fresh.schedule() == c.mask
+
+
+def test_autotune_on_first_plan(rs, cuda, at, monkeypatch):
+    monkeypatch.setenv("RS_AUTOTUNE", "1")
+    with rs._lib.plan_slot(9):
+        p = rs._lib.plan_for(768, 768, cuda)
+    assert at.cached_schedule(768, 768, cuda) == p.schedule()
+    torch.cuda.synchronize()

@@ -37,7 +37,9 @@ def test_run_history_vs_bigwave(rs, cuda):
     frames = h.get_history()
     assert frames.shape == ref.shape
     n_analytic = len(np.arange(0, 0.5, hdz)[1:])
-    np.testing.assert_array_equal(frames[:n_analytic], ref[:n_analytic])
+    # host FP64 with the reference's arithmetic; numpy's pow may differ in the last bit between
+    # CPU architectures
+    np.testing.assert_allclose(frames[:n_analytic], ref[:n_analytic], rtol=1e-14, atol=0)
     for k in range(n_analytic, len(ref)):
         assert rel_l2(frames[k], ref[k]) < 2e-5, (k, ref_z[k])
     assert rel_l2(outs[0], g["run_out"]) < 2e-5

@@ -43,7 +43,7 @@ def test_memory_history_matches_bigwave(hm, golden):
 
 def test_analytic_source_frames_match_bigwave(rs, hm, golden):
     """The first frames of the recorded run are PointSource's analytic history (host FP64,
-    big-wave/history.py:348-367): same arithmetic, so bit-identical."""
+    big-wave/history.py:348-367)."""
     a0, a1, a2, wl, hdz = golden["run_params"]
     p = rs.SimParams(N=64 * 64, nx=64, ny=64, dx=0.5e-6, dy=0.5e-6, z_detector=0.65, detector_size=24e-6,
                      detector_size_x=24e-6, detector_size_y=20e-6, detector_pixel_size_x=1.5e-6,
@@ -52,7 +52,9 @@ def test_analytic_source_frames_match_bigwave(rs, hm, golden):
     zs = np.arange(0, 0.5, hdz)[1:]
     hm.generate_analytic_history_2d(h, zs, 1e-6, 0.0, p, np.sin(a0) / wl)
     n = len(zs)
-    np.testing.assert_array_equal(h.get_history(), golden["run_history"][:n])
+    # same arithmetic as the reference; numpy's pow may round the last bit differently on
+    # another CPU architecture than the one that wrote the fixture
+    np.testing.assert_allclose(h.get_history(), golden["run_history"][:n], rtol=1e-14, atol=0)
     np.testing.assert_array_equal(np.array(h.get_z()), golden["run_history_z"][:n])
 
 
