@@ -208,10 +208,10 @@ def plain_slice_rate(rs, torch, wl, device, slices: int, use_cufft: bool) -> flo
         lib.check(L.rs_apply_transmission_voxel(plan.handle, lib.ptr(u), lib.ptr(sample.grid), 0, lib.ptr(db),
                                                 len(sample.db_list), geom, p.dx, p.dx, p.wl, k, 1.0, st), "T")
         if use_cufft:
-            Uv = torch.fft.fft2(u.view(n, n))
-            lib.check(L.rs_apply_transfer(plan.handle, lib.ptr(Uv), p.dx, p.dx, p.wl, sample.pixel_size_z,
+            torch.fft.fft2(u.view(n, n), out=U.view(n, n))
+            lib.check(L.rs_apply_transfer(plan.handle, lib.ptr(U), p.dx, p.dx, p.wl, sample.pixel_size_z,
                                           wl.cutoff, st), "H")
-            u.copy_(torch.fft.ifft2(Uv).view(-1))
+            torch.fft.ifft2(U.view(n, n), out=u.view(n, n))
         else:
             lib.check(L.rs_fft2(plan.handle, lib.ptr(u), lib.ptr(U), st), "fft2")
             lib.check(L.rs_apply_transfer(plan.handle, lib.ptr(U), p.dx, p.dx, p.wl, sample.pixel_size_z,
@@ -380,12 +380,16 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
     b = ms.shell_batch(max_items=items)
     fused = ms.BatchRunner(b, device, streams=2)  # 2 streams measured faster than 4 or 8 (0.96 vs 1.03 vs 1.05 s)
     plain = ms.BatchRunner(b, device, streams=1)
+    plain_cufft = ms.BatchRunner(b, device, streams=1)
     fused.run(b.items[:4])
     plain.run(b.items[:1], plain=True)
+    plain_cufft.run(b.items[:4], plain="cufft")  # cuFFT plans of every size
     fused.zero()
     plain.zero()
+    plain_cufft.zero()
     out = {}
-    for name, runner, kw in (("fused", fused, {}), ("plain_loop", plain, {"plain": True})):
+    for name, runner, kw in (("fused", fused, {}), ("plain_loop", plain, {"plain": True}),
+                             ("plain_loop_cufft", plain_cufft, {"plain": "cufft"})):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         runner.run(**kw)
@@ -408,7 +412,9 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
            "fused_items_per_s": round(items / out["fused_s"], 2),
            "fused_graph_items_per_s": round(items / out["fused_graph_s"], 2),
            "plain_loop_items_per_s": round(items / out["plain_loop_s"], 2),
+           "plain_loop_cufft_items_per_s": round(items / out["plain_loop_cufft_s"], 2),
            "speedup": round(out["plain_loop_s"] / min(out["fused_s"], out["fused_graph_s"]), 2),
+           "speedup_vs_cufft_loop": round(out["plain_loop_cufft_s"] / min(out["fused_s"], out["fused_graph_s"]), 2),
            "graph_capture_s": round(capture_s, 2), **out}
     return res
 

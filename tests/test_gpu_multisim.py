@@ -59,3 +59,11 @@ def test_batch_graph_replay_matches_eager_run(ms, cuda):
     second = runner.replay().clone()
     assert torch.equal(first, eager)
     assert torch.equal(second, first)
+
+
+def test_plain_loop_with_cufft_matches_own_ffts(ms, cuda):
+    """The cuFFT form of the unfused comparator computes the same batch as the fused runner."""
+    b = small_batch(ms)
+    fused = ms.BatchRunner(b, cuda, streams=2).run()
+    cufft = ms.BatchRunner(b, cuda, streams=1).run(plain="cufft")
+    assert rel_l2(cufft.cpu().numpy(), fused.cpu().numpy()) < 1e-5
