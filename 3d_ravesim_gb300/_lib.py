@@ -73,6 +73,7 @@ _SIGS = {
     "rs_detector_adjoint": ([_P, _P, _P, _P, ctypes.POINTER(DetectorGeom), _P], c_int),
     "rs_plan_set_pipeline": ([_P, c_int], c_int),
     "rs_plan_set_schedule": ([_P, c_int], c_int),
+    "rs_plan_is_four_step": ([_P], c_int),
     "rs_plan_get_schedule": ([_P, ctypes.POINTER(c_int)], c_int),
     "rs_plan_schedules": ([_P, ctypes.POINTER(c_int), c_int, ctypes.POINTER(c_int)], c_int),
     "rs_plan_status": ([_P, ctypes.POINTER(c_int)], c_int),
@@ -83,6 +84,8 @@ _SIGS = {
     "rs_apply_transmission_voxel": ([_P, _P, _P, c_int, _P, c_int, ctypes.POINTER(VoxelGeom),
                                      c_double, c_double, c_double, c_int, c_double, _P], c_int),
 }
+
+RS_PLAN_FOURSTEP = 1  # rs_plan_create flag (include/rs_fresnel.h)
 
 _lib = None
 _lock = threading.Lock()
@@ -141,13 +144,16 @@ def ptr(t: torch.Tensor) -> c_void_p:
 class Plan:
     """Owns one rs_plan (twiddles, transfer and geometry tables) for an (nx, ny) field."""
 
-    def __init__(self, nx: int, ny: int, device: torch.device):
+    def __init__(self, nx: int, ny: int, device: torch.device, flags: int = 0):
+        """flags: 0, or RS_PLAN_FOURSTEP for a four-step plan at axes of 4096..16384 (axes of
+        32768 always get one)."""
         self.nx, self.ny, self.device = int(nx), int(ny), device
         handle = c_void_p()
         with torch.cuda.device(device):
-            check(lib().rs_plan_create(self.nx, self.ny, 0, ctypes.byref(handle)), "rs_plan_create")
+            check(lib().rs_plan_create(self.nx, self.ny, int(flags), ctypes.byref(handle)), "rs_plan_create")
         self.handle = handle
         self.fast = bool(lib().rs_plan_is_fast(handle))
+        self.four_step = bool(lib().rs_plan_is_four_step(handle))
         self._finalizer = weakref.finalize(self, Plan._destroy, handle, device)
 
     def set_pipeline(self, enable: bool | int) -> None:

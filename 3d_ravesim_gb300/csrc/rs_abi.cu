@@ -63,6 +63,10 @@ std::atomic<unsigned long long> g_launches{0};
 
 bool finite_pos(double v) { return std::isfinite(v) && v > 0.0; }
 
+// Four-step plans split each axis as n = n1 * kFourN2.
+constexpr int kFourN2 = 256;
+bool four_size(int n) { return n >= 16 * kFourN2 && n <= 32768 && (n & (n - 1)) == 0; }
+
 }  // namespace
 
 namespace rs {
@@ -72,6 +76,15 @@ void note_launch(unsigned n) { g_launches.fetch_add(n, std::memory_order_relaxed
 struct rs_plan {
   int nx = 0, ny = 0, dev = 0;
   bool fast = false;
+  // Four-step plans (axes n = n1 * 256 up to 32768): each axis transform is a length-n1 column
+  // transform with the W_n twiddle fused, then a length-256 transform; the spectrum is kept in
+  // four-step storage order (frequency i / 256 + n1 * (i % 256) at entry i of an axis).
+  bool four = false;
+  float4* tw_256 = nullptr;   // stage-major table of the length-256 transforms (rows and columns)
+  float4* tw2_256 = nullptr;  // two-level table of the length-256 column transform
+  float4* tw_c1x = nullptr;   // stage-major tables of the length-n1 column transforms
+  float4* tw_c1y = nullptr;
+  int* kyi = nullptr;         // signed y-frequency index per storage row
   void* arena = nullptr;
   float4* tws_x = nullptr;  // compensated stage-major twiddles (fast sizes)
   float4* tws_y = nullptr;
@@ -128,6 +141,15 @@ int check_plan(const rs_plan* p) {
   return RS_OK;
 }
 
+// Entry points whose passes need the natural-order spectrum or the fused single-length passes.
+int check_plan_std(const rs_plan* p, const char* name) {
+  RS_TRY(check_plan(p));
+  if (p->four)
+    return fail(RS_EUNSUPPORTED, "%s: a four-step plan (%dx%d) supports rs_propagate, rs_point_source and "
+                "rs_detector only", name, p->nx, p->ny);
+  return RS_OK;
+}
+
 int build_prop(rs_plan* p, double dx, double dy, double wl, double dz, double cutoff, bool with_h,
                cudaStream_t s) {
   if (!finite_pos(dx) || !finite_pos(dy)) return fail(RS_EINVAL, "dx and dy must be positive and finite (dx=%g, dy=%g)", dx, dy);
@@ -148,6 +170,11 @@ int build_prop(rs_plan* p, double dx, double dy, double wl, double dz, double cu
   a.ex = p->ex;
   a.ey = p->ey;
   a.ylim = p->ylim;
+  if (p->four) {
+    a.n2x = kFourN2;
+    a.n2y = kFourN2;
+    a.kyi = p->kyi;
+  }
   RS_CK(launch_prop_tables(a, s));
   return RS_OK;
 }
@@ -274,6 +301,49 @@ int ifft2_impl(rs_plan* p, const float2* in, float2* out, cudaStream_t s) {
     RS_CK(launch_dft_axis(in, out, p->nx, p->ny, 1, 1, p->tw_y, 1.0f, s));
     RS_CK(launch_dft_axis(out, out, p->nx, p->ny, 0, 1, p->tw_x, inv_n, s));
   }
+  return RS_OK;
+}
+
+// propagate_2d on a four-step plan: seven passes (rs_propagate documents the order). u -> U:
+// x transforms (length-n1 columns of each row's (n1, 256) view with the W_nx twiddle, then
+// length-256 rows), the length-n1 y transforms over rows 256*m1 + m2 with the W_ny twiddle;
+// then one pass of length-256 y transforms, H, the spectrum store and the inverse; then the
+// inverse y and x steps on u. U is left holding the spectrum in four-step storage order.
+int propagate_four(rs_plan* p, float2* u, float2* U, bool skip_fft, cudaStream_t s) {
+  const int n1x = p->nx / kFourN2, n1y = p->ny / kFourN2;
+  const float inv_n = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
+  auto xcols = [&](const float2* in, float2* out, int flags) {
+    ColArgs c{};
+    c.in = in; c.out = out; c.nx = kFourN2; c.flags = flags; c.tw = p->tw_c1x;
+    c.pitch = kFourN2; c.bstride = p->nx; c.batches = p->ny; c.tw4 = p->nx; c.tw4q = 0;
+    return launch_col_pass(n1x, c, s);
+  };
+  auto xrows = [&](float2* f, int flags) {
+    RowArgs r{};
+    r.in = f; r.out = f; r.ny = p->ny * n1x; r.flags = flags; r.tw = p->tw_256;
+    return launch_row_pass(kFourN2, r, s);
+  };
+  auto ycols = [&](float2* f, int flags) {
+    ColArgs c{};
+    c.in = f; c.out = f; c.nx = p->nx; c.flags = flags; c.tw = p->tw_c1y;
+    c.pitch = static_cast<long long>(kFourN2) * p->nx; c.bstride = p->nx; c.batches = kFourN2;
+    c.tw4 = p->ny; c.tw4q = 1;
+    return launch_col_pass(n1y, c, s);
+  };
+  if (!skip_fft) {
+    RS_CK(xcols(u, U, COL_FWD));
+    RS_CK(xrows(U, ROW_FWD));
+    RS_CK(ycols(U, COL_FWD));
+  }
+  ColArgs c{};
+  c.in = U; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tw_256; c.tw2 = p->tw2_256;
+  c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.kyi = p->kyi; c.scale = inv_n;
+  c.pitch = p->nx; c.bstride = static_cast<long long>(kFourN2) * p->nx; c.batches = n1y; c.ey_bstride = kFourN2;
+  c.flags = (skip_fft ? 0 : COL_FWD) | COL_H | COL_SPEC | COL_SCALE | COL_INV;
+  RS_CK(launch_col_pass(kFourN2, c, s));
+  RS_CK(ycols(u, COL_INV));
+  RS_CK(xrows(u, ROW_INV));
+  RS_CK(xcols(u, u, COL_INV));
   return RS_OK;
 }
 
@@ -500,18 +570,23 @@ const char* rs_version(void) { return "rs_fresnel 0.1 sm_103a"; }
 const char* rs_last_error(void) { return g_err.c_str(); }
 
 int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
-  (void)flags;
   if (!out) return fail(RS_EINVAL, "out is NULL");
   *out = nullptr;
+  if (flags & ~RS_PLAN_FOURSTEP) return fail(RS_EINVAL, "unknown plan flags 0x%x", flags);
   if (nx <= 0 || ny <= 0) return fail(RS_EINVAL, "nx and ny must be positive, got nx=%d, ny=%d", nx, ny);
-  const bool fast = fast_size(nx) && fast_size(ny);
-  if (!fast && (nx > kGenericMax || ny > kGenericMax))
-    return fail(RS_EUNSUPPORTED, "size %dx%d: axes must be powers of two in [16, 16384] or at most %d",
+  // four-step when asked for, and for axes beyond the single-pass transforms (32768)
+  const bool four = four_size(nx) && four_size(ny) && ((flags & RS_PLAN_FOURSTEP) || nx > 16384 || ny > 16384);
+  if ((flags & RS_PLAN_FOURSTEP) && !four)
+    return fail(RS_EUNSUPPORTED, "size %dx%d: four-step plans need power-of-two axes in [4096, 32768]", nx, ny);
+  const bool fast = !four && fast_size(nx) && fast_size(ny);
+  if (!fast && !four && (nx > kGenericMax || ny > kGenericMax))
+    return fail(RS_EUNSUPPORTED, "size %dx%d: axes must be powers of two in [16, 32768] or at most %d",
                 nx, ny, kGenericMax);
   rs_plan* p = new rs_plan();
   p->nx = nx;
   p->ny = ny;
   p->fast = fast;
+  p->four = four;
   cudaError_t e = cudaGetDevice(&p->dev);
   if (e != cudaSuccess) { delete p; return fail(RS_ECUDA, "cudaGetDevice: %s", cudaGetErrorString(e)); }
   // One arena per plan. Fast sizes: compensated stage-major twiddles per axis (float4) and the
@@ -520,7 +595,12 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   const size_t twx = fast ? std::max(stage_twiddle_len(nx), 1) : 0;
   const size_t twy = fast ? std::max(stage_twiddle_len(ny), 1) : 0;
   const size_t tw2y = fast ? static_cast<size_t>(twiddles_2l_len(ny)) : 0;
-  const size_t gx = fast ? 0 : nx, gy = fast ? 0 : ny;
+  const size_t gx = (fast || four) ? 0 : nx, gy = (fast || four) ? 0 : ny;
+  const size_t n1x = four ? nx / kFourN2 : 0, n1y = four ? ny / kFourN2 : 0;
+  const size_t f256 = four ? std::max(stage_twiddle_len(kFourN2), 1) : 0;
+  const size_t f2l = four ? static_cast<size_t>(twiddles_2l_len(kFourN2)) : 0;
+  const size_t f1x = four ? std::max(stage_twiddle_len(static_cast<int>(n1x)), 1) : 0;
+  const size_t f1y = four ? std::max(stage_twiddle_len(static_cast<int>(n1y)), 1) : 0;
   size_t bytes = 0;
   auto take = [&](size_t n) { const size_t at = bytes; bytes += (n + 15) & ~static_cast<size_t>(15); return at; };
   const size_t o_twx = take(sizeof(float4) * twx), o_twy = take(sizeof(float4) * twy);
@@ -530,6 +610,9 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   const size_t o_ylim = take(sizeof(int) * nx), o_xi = take(sizeof(int) * nx), o_xf = take(sizeof(float) * nx);
   const size_t o_yi = take(sizeof(int) * ny), o_yf = take(sizeof(float) * ny), o_xp = take(sizeof(int2) * nx);
   const size_t o_status = take(sizeof(int));
+  const size_t o_f256 = take(sizeof(float4) * f256), o_f2l = take(sizeof(float4) * f2l);
+  const size_t o_f1x = take(sizeof(float4) * f1x), o_f1y = take(sizeof(float4) * f1y);
+  const size_t o_kyi = take(four ? sizeof(int) * ny : 0);
   e = cudaMalloc(&p->arena, bytes);
   if (e != cudaSuccess) { delete p; return fail(RS_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
   char* c = static_cast<char*>(p->arena);
@@ -537,6 +620,12 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
     p->tws_x = reinterpret_cast<float4*>(c + o_twx);
     p->tws_y = reinterpret_cast<float4*>(c + o_twy);
     if (tw2y) p->tw2_y = reinterpret_cast<float4*>(c + o_tw2y);
+  } else if (four) {
+    p->tw_256 = reinterpret_cast<float4*>(c + o_f256);
+    if (f2l) p->tw2_256 = reinterpret_cast<float4*>(c + o_f2l);
+    p->tw_c1x = reinterpret_cast<float4*>(c + o_f1x);
+    p->tw_c1y = reinterpret_cast<float4*>(c + o_f1y);
+    p->kyi = reinterpret_cast<int*>(c + o_kyi);
   } else {
     p->tw_x = reinterpret_cast<float2*>(c + o_gx);
     p->tw_y = reinterpret_cast<float2*>(c + o_gy);
@@ -559,9 +648,16 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
     p->pipe_rows = v == "1" || v == "rows";
     p->pipe_cols = v == "1" || v == "cols";
   }
-  e = fast ? launch_stage_twiddles(nx, p->tws_x, 0) : launch_twiddles(p->tw_x, nx, 0);
-  if (e == cudaSuccess) e = fast ? launch_stage_twiddles(ny, p->tws_y, 0) : launch_twiddles(p->tw_y, ny, 0);
-  if (e == cudaSuccess && p->tw2_y) e = launch_twiddles_2l(ny, p->tw2_y, 0);
+  if (four) {
+    e = launch_stage_twiddles(kFourN2, p->tw_256, 0);
+    if (e == cudaSuccess && p->tw2_256) e = launch_twiddles_2l(kFourN2, p->tw2_256, 0);
+    if (e == cudaSuccess) e = launch_stage_twiddles(static_cast<int>(n1x), p->tw_c1x, 0);
+    if (e == cudaSuccess) e = launch_stage_twiddles(static_cast<int>(n1y), p->tw_c1y, 0);
+  } else {
+    e = fast ? launch_stage_twiddles(nx, p->tws_x, 0) : launch_twiddles(p->tw_x, nx, 0);
+    if (e == cudaSuccess) e = fast ? launch_stage_twiddles(ny, p->tws_y, 0) : launch_twiddles(p->tw_y, ny, 0);
+    if (e == cudaSuccess && p->tw2_y) e = launch_twiddles_2l(ny, p->tw2_y, 0);
+  }
   if (e == cudaSuccess) e = cudaMemsetAsync(p->status, 0, sizeof(int), 0);
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   if (e != cudaSuccess) {
@@ -588,6 +684,8 @@ int rs_plan_destroy(rs_plan* p) {
 }
 
 int rs_plan_is_fast(const rs_plan* p) { return p && p->fast ? 1 : 0; }
+
+int rs_plan_is_four_step(const rs_plan* p) { return p && p->four ? 1 : 0; }
 
 int rs_plan_set_pipeline(rs_plan* p, int mask) {
   RS_TRY(check_plan(p));
@@ -674,19 +772,19 @@ int rs_plan_profile_read(rs_plan* p, double* row_ms, double* col_ms, int* n_row,
 }
 
 int rs_fft2(rs_plan* p, const void* in, void* out, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_fft2"));
   if (!in || !out) return fail(RS_EINVAL, "NULL field pointer");
   return fft2_impl(p, static_cast<const float2*>(in), static_cast<float2*>(out), as_stream(stream));
 }
 
 int rs_ifft2(rs_plan* p, const void* in, void* out, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_ifft2"));
   if (!in || !out) return fail(RS_EINVAL, "NULL field pointer");
   return ifft2_impl(p, static_cast<const float2*>(in), static_cast<float2*>(out), as_stream(stream));
 }
 
 int rs_apply_cutoff(rs_plan* p, void* U, double freq, double dx, double dy, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_apply_cutoff"));
   if (!U) return fail(RS_EINVAL, "NULL field pointer");
   cudaStream_t s = as_stream(stream);
   RS_TRY(build_prop(p, dx, dy, 1.0, 0.0, freq, false, s));
@@ -696,7 +794,7 @@ int rs_apply_cutoff(rs_plan* p, void* U, double freq, double dx, double dy, void
 
 int rs_apply_transfer(rs_plan* p, void* U, double dx, double dy, double wl, double dz, double cutoff,
                       void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_apply_transfer"));
   if (!U) return fail(RS_EINVAL, "NULL field pointer");
   cudaStream_t s = as_stream(stream);
   RS_TRY(build_prop(p, dx, dy, wl, dz, cutoff, true, s));
@@ -712,6 +810,7 @@ int rs_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double wl
   float2* U = static_cast<float2*>(U_);
   cudaStream_t s = as_stream(stream);
   RS_TRY(build_prop(p, dx, dy, wl, dz, cutoff, true, s));
+  if (p->four) return propagate_four(p, u, U, skip_fft != 0, s);
   if (p->fast) {
     const float inv_n = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
     if (!skip_fft) {
@@ -763,7 +862,7 @@ static int source_propagate(rs_plan* p, void* u_, void* U_, const PointSrcArgs& 
 
 int rs_point_source_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double xs,
                               double ys, double z, double wl, double cutoff, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_point_source_propagate"));
   if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
   PointSrcArgs a{};
   RS_TRY(point_args(p, dx, dy, xs, ys, z, wl, a));
@@ -785,7 +884,7 @@ int rs_fresnel_plane(rs_plan* p, void* u, double dx, double dy, double xs, doubl
 
 int rs_fresnel_plane_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double xs, double ys,
                                double dz, double wl, double cutoff, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_fresnel_plane_propagate"));
   if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
   if (!(dz > 0.0) || !std::isfinite(dz)) return fail(RS_EINVAL, "Fresnel source-to-sample distance must be positive");
   PointSrcArgs a{};
@@ -826,7 +925,7 @@ int rs_multislice_voxel(rs_plan* p, void* u, void* U, const void* grid, int grid
                         int n_db, const rs_voxel_geom* geom, double dx, double dy, double wl,
                         double cutoff, const double* slice_dz, const double* coord_scale,
                         int slice_begin, int slice_end, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_multislice_voxel"));
   if (!grid || !db) return fail(RS_EINVAL, "grid and db must be device pointers");
   if (n_db < 1) return fail(RS_EINVAL, "n_db must be >= 1");
   SliceSource src;
@@ -843,7 +942,7 @@ int rs_multislice_plasma(rs_plan* p, void* u, void* U, const void* ne, const voi
                          const rs_voxel_geom* geom, double dx, double dy, double wl, double cutoff,
                          const double* slice_dz, const double* coord_scale, int slice_begin,
                          int slice_end, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_multislice_plasma"));
   if (!ne || !ni || !te || !zstar) return fail(RS_EINVAL, "plasma grids must be device pointers");
   if (!pc || !finite_pos(pc->energy_ev)) return fail(RS_EINVAL, "energy must be positive");
   SliceSource src;
@@ -872,7 +971,7 @@ int rs_multislice_plasma(rs_plan* p, void* u, void* U, const void* ne, const voi
 int rs_multislice_dbgrid(rs_plan* p, void* u, void* U, const float* db_grid, const rs_voxel_geom* geom,
                          double dx, double dy, double wl, double cutoff, const double* slice_dz,
                          const double* coord_scale, int slice_begin, int slice_end, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_multislice_dbgrid"));
   if (!db_grid) return fail(RS_EINVAL, "db_grid must be a device pointer");
   SliceSource src;
   src.dbv = reinterpret_cast<const float2*>(db_grid);
@@ -885,7 +984,7 @@ int rs_multislice_dbgrid_store(rs_plan* p, void* u, void* U, const float* db_gri
                                double dx, double dy, double wl, double cutoff, const double* slice_dz,
                                const double* coord_scale, int slice_begin, int slice_end, void* fields,
                                void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_multislice_dbgrid_store"));
   if (!db_grid || !fields) return fail(RS_EINVAL, "db_grid and fields must be device pointers");
   if (!p->fast) return fail(RS_EUNSUPPORTED, "field storing needs the fused passes (fast sizes)");
   SliceSource src;
@@ -900,7 +999,7 @@ int rs_adjoint_multislice_dbgrid(rs_plan* p, void* g, const float* db_grid, cons
                                  double dy, double wl, double cutoff, const double* slice_dz,
                                  const double* coord_scale, int slice_begin, int slice_end, const void* fields,
                                  float* grad_grid, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_adjoint_multislice_dbgrid"));
   if (!g || !db_grid || !fields || !grad_grid || !geom || !slice_dz) return fail(RS_EINVAL, "NULL pointer argument");
   if (geom->nz <= 0 || geom->ny_v < 2 || geom->nx_v < 2) return fail(RS_EINVAL, "bad grid shape");
   if (slice_begin < 0 || slice_end > geom->nz || slice_begin > slice_end)
@@ -957,7 +1056,7 @@ int rs_adjoint_multislice_dbgrid(rs_plan* p, void* g, const float* db_grid, cons
 int rs_adjoint_slice(rs_plan* p, void* v, const void* u, const float* db_grid, const rs_voxel_geom* g,
                      double dx, double dy, double wl, int slice, double coord_scale, float* grad_grid,
                      void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_adjoint_slice"));
   if (!v || !u || !db_grid || !grad_grid || !g) return fail(RS_EINVAL, "NULL pointer argument");
   if (slice < 0 || slice >= g->nz) return fail(RS_EINVAL, "slice %d outside [0, %d)", slice, g->nz);
   if (g->ny_v < 2 || g->nx_v < 2) return fail(RS_EINVAL, "bad grid shape");
@@ -983,7 +1082,7 @@ int rs_adjoint_slice(rs_plan* p, void* v, const void* u, const float* db_grid, c
 
 int rs_detector_adjoint(rs_plan* p, const void* u, void* g_out, const double* r, const rs_detector_geom* g,
                         void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_detector_adjoint"));
   if (!u || !g_out || !r || !g) return fail(RS_EINVAL, "NULL pointer argument");
   if (g->out_x <= 0 || g->out_y <= 0) return fail(RS_EINVAL, "detector output must be non-empty");
   if (!finite_pos(g->dx) || !finite_pos(g->dy) || !finite_pos(g->ds_px) || !finite_pos(g->ds_py))
@@ -1072,7 +1171,7 @@ int rs_detector_adjoint(rs_plan* p, const void* u, void* g_out, const double* r,
 int rs_apply_transmission_voxel(rs_plan* p, void* u, const void* grid, int grid_signed, const float* db,
                                 int n_db, const rs_voxel_geom* g, double dx, double dy, double wl,
                                 int slice, double coord_scale, void* stream) {
-  RS_TRY(check_plan(p));
+  RS_TRY(check_plan_std(p, "rs_apply_transmission_voxel"));
   if (!u || !grid || !db || !g) return fail(RS_EINVAL, "NULL pointer argument");
   if (slice < 0 || slice >= g->nz) return fail(RS_EINVAL, "slice %d outside [0, %d)", slice, g->nz);
   if (g->ny_v < 2 || g->nx_v < 2 || n_db < 1) return fail(RS_EINVAL, "bad grid shape or table");

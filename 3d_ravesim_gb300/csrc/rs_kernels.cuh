@@ -98,6 +98,17 @@ struct ColArgs {
   const float2* ey;      // ny entries: exp(2 pi i dz/wl) * exp(-i pi wl dz ky^2)
   const int* ylim;       // nx entries: largest |signed y index| kept by the cutoff, -1 = none
   const float4* tw2;     // two-level twiddle table of length ny (Fft2L), when ny has one
+  // Batched and strided transforms (the per-block kernel only; all zero for a plain field):
+  long long pitch;       // elements between consecutive rows of a transform; 0 = nx
+  long long bstride;     // elements between the transforms of consecutive blockIdx.y
+  int batches;           // blockIdx.y range (0 = 1)
+  int ey_bstride;        // ey / kyi entries between consecutive blockIdx.y
+  const int* kyi;        // signed y-frequency index per storage row (null: natural order)
+  // Four-step twiddle W_L^{p*q} (W_L = exp(-2 pi i/L)), p = the transform position of the value,
+  // q = the column (tw4q = 0) or blockIdx.y (tw4q = 1): multiplied after a forward transform,
+  // conjugated before an inverse one. L = tw4, a power of two <= 32768; 0 = none.
+  int tw4;
+  int tw4q;
 };
 
 // ----------------------------------------------------------------------------- physics
@@ -623,15 +634,34 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T, (W * FftPlan<N>::T <= 512 ?
   const int flags = a.flags;
   constexpr int E = P::E;
   float2 v[E];
+  // batched / strided transforms: this block's transform starts at blockIdx.y * bstride
+  const size_t pitch = a.pitch ? static_cast<size_t>(a.pitch) : static_cast<size_t>(nx);
+  const size_t boff = static_cast<size_t>(blockIdx.y) * static_cast<size_t>(a.bstride);
+  const float2* in = a.in + boff;
+  float2* out = a.out + boff;
+  const int yrow0 = blockIdx.y * a.ey_bstride;
 
   if (flags & COL_FWD) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = a.in[static_cast<size_t>(slot_pos<N, RF>(t, e)) * nx + x];
+    for (int e = 0; e < E; ++e) v[e] = in[static_cast<size_t>(slot_pos<N, RF>(t, e)) * pitch + x];
     if constexpr (L2) fft2l_fwd<N, PadAddr, PadAddr, 1, TwGlobal>(v, buf, t, a.tw2);
     else fft_seq<N, false>(v, buf, t, a.tw);
   } else {
 #pragma unroll
-    for (int e = 0; e < E; ++e) v[e] = a.in[static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * nx + x];
+    for (int e = 0; e < E; ++e) v[e] = in[static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * pitch + x];
+  }
+  if (a.tw4) {
+    // registers hold transform positions fy (forward exit == inverse entry mapping); the angle
+    // -2 pi (fy*q mod L)/L is exact in float (L <= 2^15), so sincospif gets an exact argument
+    const int q = a.tw4q ? static_cast<int>(blockIdx.y) : x;
+    const float inv_half = 2.0f / static_cast<float>(a.tw4);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const int pq = (col_exit_pos<N, L2>(t, e) * q) & (a.tw4 - 1);
+      float sn, cs;
+      sincospif(-static_cast<float>(pq) * inv_half, &sn, &cs);
+      v[e] = cmul(v[e], make_float2(cs, (flags & COL_FWD) ? sn : -sn));
+    }
   }
 
   // registers are in the forward-exit (== inverse-entry) mapping: position = fy; with H applied
@@ -643,19 +673,20 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T, (W * FftPlan<N>::T <= 512 ?
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int fy = col_exit_pos<N, L2>(t, e);
-      const int m = fy < (N + 1) / 2 ? fy : fy - N;
+      const int yr = yrow0 + fy;  // storage row of the table entries
+      const int m = a.kyi ? __ldg(&a.kyi[yr]) : (fy < (N + 1) / 2 ? fy : fy - N);
       const bool keep = (m < 0 ? -m : m) <= lim;
       if (!keep) {
         v[e] = make_float2(0.f, 0.f);
       } else if (flags & COL_H) {
-        const float2 eyv = fold ? cscale(__ldg(&a.ey[fy]), a.scale) : __ldg(&a.ey[fy]);
+        const float2 eyv = fold ? cscale(__ldg(&a.ey[yr]), a.scale) : __ldg(&a.ey[yr]);
         v[e] = cmul(v[e], cmul(exv, eyv));
       }
     }
   }
   if ((flags & COL_SPEC) && live) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * nx + x] = v[e];
+    for (int e = 0; e < E; ++e) a.spec[boff + static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * pitch + x] = v[e];
   }
   if ((flags & COL_SCALE) && !fold) {
 #pragma unroll
@@ -666,11 +697,11 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T, (W * FftPlan<N>::T <= 512 ?
     else fft_seq<N, true>(v, buf, t, a.tw);
     if (live) {
 #pragma unroll
-      for (int e = 0; e < E; ++e) a.out[static_cast<size_t>(slot_pos<N, RF>(t, e)) * nx + x] = v[e];
+      for (int e = 0; e < E; ++e) out[static_cast<size_t>(slot_pos<N, RF>(t, e)) * pitch + x] = v[e];
     }
   } else if (live) {
 #pragma unroll
-    for (int e = 0; e < E; ++e) a.out[static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * nx + x] = v[e];
+    for (int e = 0; e < E; ++e) out[static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * pitch + x] = v[e];
   }
 }
 

@@ -37,10 +37,15 @@ __device__ __forceinline__ int signed_index(int i, int n) {
   return i < (n - 1) / 2 + 1 ? i : i - n;
 }
 
+// Frequency index held by storage entry i of an axis of length n (four-step order when n2 > 0).
+__device__ __forceinline__ int storage_freq(int i, int n, int n2) {
+  return n2 > 0 ? i / n2 + (n / n2) * (i % n2) : i;
+}
+
 __global__ void prop_tables_kernel(const PropTabArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < a.nx) {
-    const int mx = signed_index(i, a.nx);
+    const int mx = signed_index(storage_freq(i, a.nx, a.n2x), a.nx);
     const double kx2 = kfreq2_abs(mx < 0 ? -mx : mx, a.nx, a.dx);
     if (a.with_h) {
       double s, c;
@@ -60,8 +65,9 @@ __global__ void prop_tables_kernel(const PropTabArgs a) {
     }
     a.ylim[i] = lim;
   }
+  if (a.kyi && i < a.ny) a.kyi[i] = signed_index(storage_freq(i, a.ny, a.n2y), a.ny);
   if (a.with_h && i < a.ny) {
-    const int my = signed_index(i, a.ny);
+    const int my = signed_index(storage_freq(i, a.ny, a.n2y), a.ny);
     const double ky2 = kfreq2_abs(my < 0 ? -my : my, a.ny, a.dy);
     double s, c, gs, gc;
     sincos(__dmul_rn(a.ps, ky2), &s, &c);

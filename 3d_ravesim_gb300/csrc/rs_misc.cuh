@@ -15,6 +15,10 @@ struct PropTabArgs {
   float2* ex;
   float2* ey;
   int* ylim;
+  // Four-step storage order (0 = natural): entry i of an axis of length n describes frequency
+  // i / n2 + (n / n2) * (i % n2), the order the four-step transforms leave the spectrum in.
+  int n2x, n2y;
+  int* kyi;        // with n2y: signed y-frequency index of each storage row
 };
 
 // Sample coordinate table for one axis (big-wave/optical_element.py:538-546, 555-563).

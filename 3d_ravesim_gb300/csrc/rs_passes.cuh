@@ -161,7 +161,8 @@ cudaError_t launch_cols_nw(const ColArgs& a, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     configured |= bit;
   }
-  col_pass_kernel<N, W><<<(a.nx + W - 1) / W, G::THREADS, G::SMEM, s>>>(a);
+  const dim3 grid((a.nx + W - 1) / W, a.batches > 0 ? a.batches : 1);
+  col_pass_kernel<N, W><<<grid, G::THREADS, G::SMEM, s>>>(a);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) note_launch();
   return e;

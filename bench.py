@@ -419,6 +419,56 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
     return res
 
 
+def sweep_32768(rs, torch, device, reps: int = 5) -> dict:
+    """One FFT + propagate sweep at 32768^2 complex64 (8 GiB per field, the large-field case's
+    roofline check): rs_propagate on a four-step plan, 30 keV, 50 nm pixels, 0.5 um step, the
+    circular cutoff active. The field (8 GiB) is far larger than L2, so no flush is needed."""
+    n = 32768
+    lib = rs._lib
+    plan = lib.plan_for(n, n, device)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    u = torch.polar(torch.ones(n * n // 64), torch.rand(n * n // 64, generator=g) * 6.283).to(torch.complex64)
+    u = u.to(device).repeat(64)
+    U = torch.empty_like(u)
+    dx, wl = 50e-9, rs.convert_energy_wavelength(30000.0)
+    f = 0.45 / dx
+    st = lib.stream_handle()
+    L = lib.lib()
+
+    def step(skip):
+        lib.check(L.rs_propagate(plan.handle, lib.ptr(u), lib.ptr(U), dx, dx, wl, 0.5e-6, f, skip, st), "propagate")
+
+    step(0)
+    step(1)
+    torch.cuda.synchronize()
+    out = {}
+    for skip, name in ((0, "fft_propagate"), (1, "propagate_skip_fft")):
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            step(skip)
+            b.record()
+            b.synchronize()
+            ts.append(a.elapsed_time(b))
+        ms = float(np.median(ts))
+        passes = 7 if skip == 0 else 4
+        out[name] = {"ms": round(ms, 3), "passes": passes,
+                     "pass_traffic_GB_s": round(passes * 16 * n * n / (ms * 1e-3) / 1e9, 1),
+                     "slice_step_GB_s": round(32 * n * n / (ms * 1e-3) / 1e9, 1)}
+    peak, kind = measured_peak_hbm()
+    for v in out.values():
+        v["pass_traffic_frac"] = round(v["pass_traffic_GB_s"] / peak, 3)
+        v["slice_step_frac"] = round(v["slice_step_GB_s"] / peak, 3)
+    del u, U
+    torch.cuda.empty_cache()
+    return {"case": "32768^2 c64 four-step plan (length-128 and length-256 transforms per axis), "
+                    "30 keV, 50 nm pixels, dz 0.5 um, cutoff 0.45/dx",
+            "peak_GB_s": peak, "peak_kind": kind,
+            "slice_step_bytes": "32 B per pixel (2 field round trips, the single-pass minimum)",
+            "pass_bytes": "16 B per pixel per pass", **out}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -583,6 +633,7 @@ def run_ours(args):
         line["plasma_forward"] = plasma_forward_rate(rs, torch, device)
         line["adjoint"] = [adjoint_cost(rs, torch, device), adjoint_cost(rs, torch, device, checkpoint_every=0)]
         line["multisim"] = multisim_cost(rs, torch, device)
+        line["sweep_32768"] = sweep_32768(rs, torch, device)
         line["cpu_baseline"] = cpu_baseline(n)
         # the full slice count at 1024^2 (errors that repeat every slice add up over 514 of them),
         # and the benchmark size itself truncated to 4 sample slices

@@ -52,11 +52,21 @@ const char* rs_last_error(void);
 /* Create a plan for fields of nx columns by ny rows on the current CUDA device.
  * Replaces the per-call setup of big-wave/propagation.py:396-442 (fftfreq tables,
  * chunk validation) and fast-wave's FFT<S> plan (fast-wave/src/fft.cpp:6-28).
- * flags: reserved, pass 0. */
+ * Axes of 2^k in [16, 16384] or 3*2^k in [24, 12288] get the single-pass fused transforms;
+ * other axes up to 6144 the direct DFT. Axes of 32768 (both axes powers of two in
+ * [4096, 32768]) get a four-step plan: each axis transform runs as a length-n/256 transform
+ * with the W_n twiddle fused, then a length-256 transform, and the spectrum is kept in
+ * four-step storage order (entry i of an axis holds frequency i/256 + (n/256)*(i%256)).
+ * A four-step plan serves rs_propagate (U is left in that order; skip_fft expects it),
+ * rs_point_source and rs_detector; the other entry points return RS_EUNSUPPORTED.
+ * flags: 0, or RS_PLAN_FOURSTEP to ask for a four-step plan at 4096..16384 as well. */
+#define RS_PLAN_FOURSTEP 1u
 int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out);
 int rs_plan_destroy(rs_plan* plan);
 /* 1 when both axes use the fused Stockham kernels, 0 when the generic DFT path is used. */
 int rs_plan_is_fast(const rs_plan* plan);
+/* 1 if the plan is a four-step plan (see rs_plan_create), else 0. */
+int rs_plan_is_four_step(const rs_plan* plan);
 
 /* Unnormalised forward 2D DFT, out may equal in.
  * Replaces NumpyVector.fft2 = scipy.fft.fft2 (big-wave/vector.py:341-343). */

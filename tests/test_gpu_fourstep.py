@@ -1,0 +1,117 @@
+"""Four-step plans (axes up to 32768): rs_propagate through the length-n/256 and length-256
+transforms against the single-pass plan and the FP64 oracle at 4096/8192, the spectrum in
+four-step storage order, skip_fft chaining, and at 32768^2 the dz / -dz round trip and
+Parseval (no FP64 reference fits the host there)."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def storage_to_natural(n: int) -> np.ndarray:
+    """Frequency held by storage entry i of an axis of length n."""
+    i = np.arange(n)
+    return i // 256 + (n // 256) * (i % 256)
+
+
+def natural_spectrum(U: np.ndarray) -> np.ndarray:
+    ny, nx = U.shape
+    out = np.empty_like(U)
+    out[np.ix_(storage_to_natural(ny), storage_to_natural(nx))] = U
+    return out
+
+
+def propagate(rs, plan, u, U, dx, dy, wl, dz, f, skip=0):
+    rs._lib.check(rs._lib.lib().rs_propagate(plan.handle, rs._lib.ptr(u), rs._lib.ptr(U), dx, dy, wl, dz, f, skip,
+                                             rs._lib.stream_handle()), "rs_propagate")
+
+
+def field(n_y, n_x, seed, device):
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    re = torch.randn(n_y * n_x, generator=g)
+    ph = torch.rand(n_y * n_x, generator=g) * 6.283
+    return torch.polar(1 + 0.1 * re, ph).to(torch.complex64).to(device)
+
+
+@pytest.mark.parametrize("nx,ny", [(4096, 4096), (8192, 4096), (4096, 16384)])
+def test_four_step_matches_single_pass(rs, cuda, nx, ny):
+    lib = rs._lib
+    four = lib.Plan(nx, ny, cuda, flags=lib.RS_PLAN_FOURSTEP)
+    std = lib.Plan(nx, ny, cuda)
+    assert four.four_step and not std.four_step and std.fast
+    dx, dy, wl = 0.1e-6, 0.12e-6, 5e-11
+    f = 0.4 / dx  # active cutoff
+    u0 = field(ny, nx, 11, cuda)
+    u1, U1 = u0.clone(), torch.empty_like(u0)
+    u2, U2 = u0.clone(), torch.empty_like(u0)
+    with torch.cuda.device(cuda):
+        propagate(rs, four, u1, U1, dx, dy, wl, 2e-3, f)
+        propagate(rs, std, u2, U2, dx, dy, wl, 2e-3, f)
+    torch.cuda.synchronize()
+    # both FP32; the four-step W_n twiddles are sincospif values, the single-pass ones compensated
+    assert rel_l2(u1.cpu().numpy(), u2.cpu().numpy()) < 4e-6
+    Un = natural_spectrum(U1.cpu().numpy().reshape(ny, nx))
+    assert rel_l2(Un, U2.cpu().numpy().reshape(ny, nx)) < 4e-6
+    # a second step from the stored spectrum (skip_fft) continues both the same way
+    with torch.cuda.device(cuda):
+        propagate(rs, four, u1, U1, dx, dy, wl, 1e-3, f, skip=1)
+        propagate(rs, std, u2, U2, dx, dy, wl, 1e-3, f, skip=1)
+    torch.cuda.synchronize()
+    assert rel_l2(u1.cpu().numpy(), u2.cpu().numpy()) < 6e-6
+
+
+def test_four_step_vs_fp64_oracle(rs, cuda, oracle):
+    nx = ny = 4096
+    lib = rs._lib
+    four = lib.Plan(nx, ny, cuda, flags=lib.RS_PLAN_FOURSTEP)
+    dx, wl = 0.1e-6, rs.convert_energy_wavelength(25000.0)
+    f = 0.45 / dx
+    u0 = field(ny, nx, 5, cuda)
+    u, U = u0.clone(), torch.empty_like(u0)
+    with torch.cuda.device(cuda):
+        propagate(rs, four, u, U, dx, dx, wl, 0.01, f)
+    ref, _ = oracle.propagate_2d(u0.cpu().numpy().astype(np.complex128).reshape(ny, nx), dx, dx, wl, 0.01, f)
+    assert rel_l2(u.cpu().numpy().reshape(ny, nx), ref) < 1e-5
+
+
+def test_four_step_rejects_other_entry_points(rs, cuda):
+    lib = rs._lib
+    four = lib.Plan(4096, 4096, cuda, flags=lib.RS_PLAN_FOURSTEP)
+    u = torch.zeros(4096 * 4096, dtype=torch.complex64, device=cuda)
+    rc = lib.lib().rs_fft2(four.handle, lib.ptr(u), lib.ptr(u), lib.stream_handle())
+    assert rc != 0 and b"four-step" in lib.lib().rs_last_error()
+    with pytest.raises(Exception):
+        lib.Plan(4096, 3072, cuda, flags=lib.RS_PLAN_FOURSTEP)
+
+
+def test_32768_round_trip_and_parseval(rs, cuda):
+    """The 32768^2 sweep: propagate by dz with the cutoff inactive keeps the field's norm
+    (Parseval, the transfer function has modulus 1), and -dz brings the field back."""
+    n = 32768
+    p = rs.SimParams(N=n * n, nx=n, ny=n, dx=50e-9, dy=50e-9, z_detector=1.0, detector_size=n * 50e-9,
+                     detector_pixel_size_x=50e-9 * 64, detector_pixel_size_y=50e-9 * 64,
+                     wl=rs.convert_energy_wavelength(30000.0), chunk_size=n)
+    plan = rs._lib.plan_for(n, n, cuda)
+    assert plan.four_step
+    u = rs.GpuVector(field(n, n, 3, cuda))
+    u0 = u.vec.clone()
+    U = rs.GpuVector.zeros(n * n, cuda)
+    f = 1.0 / p.dx  # 2 f^2 above every kx^2 + ky^2: no frequency is cut
+    rs.propagate_2d(u, U, p.dx, p.dy, p.wl, 1e-4, p.chunk_size, f, n, n)
+    n0 = torch.linalg.vector_norm(u0.to(torch.complex128)).item()
+    n1 = torch.linalg.vector_norm(u.vec.to(torch.complex128)).item()
+    assert abs(n1 / n0 - 1) < 2e-6
+    assert (u.vec - u0).abs().max().item() > 1e-3  # the step did something
+    rs.propagate_2d(u, U, p.dx, p.dy, p.wl, -1e-4, p.chunk_size, f, n, n)
+    err = (torch.linalg.vector_norm((u.vec - u0).to(torch.complex128)) / n0).item()
+    assert err < 2e-5
+    # detector on the four-step plan's (natural-order) field
+    img = rs.square_and_downsample_2d(u, p, 1.0)
+    assert img.shape == (512, 512) and np.isfinite(img).all()
+    del u, U, u0
+    torch.cuda.empty_cache()
