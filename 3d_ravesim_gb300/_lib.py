@@ -164,7 +164,8 @@ class Plan:
             check(lib().rs_plan_set_pipeline(self.handle, mask), "rs_plan_set_pipeline")
 
     def set_schedule(self, mask: int) -> None:
-        """Pass schedule bits: 1 pipelined rows, 2 pipelined columns, 4 general row kernel."""
+        """Pass schedule bits: 1 pipelined rows, 2 pipelined columns, 4 general row kernel,
+        8 split (three-pass) columns."""
         with torch.cuda.device(self.device):
             check(lib().rs_plan_set_schedule(self.handle, int(mask)), "rs_plan_set_schedule")
 

@@ -3,7 +3,8 @@
 Every fast size has several schedules of the two fused passes (`Plan.schedules()`, bits of
 `Plan.set_schedule`): the column passes as one block per strip of columns or as the persistent
 TMA-box pipeline; the row passes as one block per row group (with or without the voxel-only
-specialisation) or as the persistent bulk-copy pipeline. All compute the same transform; which
+specialisation) or as the persistent bulk-copy pipeline; for 4096..16384-point columns, the
+column pass may also run as three shorter four-step passes. All compute the same transform; which
 is fastest depends on the size (threads per transform, shared memory per strip,
 resident blocks). `tune_multislice` times each schedule on a seeded multislice run of the
 size (CUDA events on the launching stream, median of `reps`), measures each schedule's field

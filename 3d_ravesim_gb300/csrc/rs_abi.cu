@@ -84,7 +84,15 @@ struct rs_plan {
   float4* tw2_256 = nullptr;  // two-level table of the length-256 column transform
   float4* tw_c1x = nullptr;   // stage-major tables of the length-n1 column transforms
   float4* tw_c1y = nullptr;
+  float4* tw4x = nullptr;     // W_n^m tables of the fused four-step twiddles (compensated)
+  float4* tw4y = nullptr;
   int* kyi = nullptr;         // signed y-frequency index per storage row
+  // Split columns (fast plans with ny = n1 * 256 in [4096, 16384]): the fused column pass of a
+  // multislice step as three passes (length-n1 forward with W_ny, length-256 forward / H /
+  // inverse, length-n1 inverse), selected by RS_SCHED_SPLIT_COLS.
+  bool split_ok = false;
+  bool split_cols = false;
+  float2* ey_s = nullptr;     // ey in four-step storage order
   void* arena = nullptr;
   float4* tws_x = nullptr;  // compensated stage-major twiddles (fast sizes)
   float4* tws_y = nullptr;
@@ -176,6 +184,15 @@ int build_prop(rs_plan* p, double dx, double dy, double wl, double dz, double cu
     a.kyi = p->kyi;
   }
   RS_CK(launch_prop_tables(a, s));
+  if (p->split_ok && with_h) {  // ey and the frequency index of each row in four-step order
+    PropTabArgs b = a;
+    b.ex = nullptr;
+    b.ylim = nullptr;
+    b.ey = p->ey_s;
+    b.kyi = p->kyi;
+    b.n2y = kFourN2;
+    RS_CK(launch_prop_tables(b, s));
+  }
   return RS_OK;
 }
 
@@ -235,7 +252,31 @@ cudaError_t run_row(rs_plan* p, const RowArgs& r, cudaStream_t s) {
   return launch_row_pass(p->nx, r, s, p->row_vox);
 }
 
+// The fused column pass of a multislice step (FWD | H | SCALE | INV, no spectrum store) as three
+// four-step passes over the y axis; rows come back in natural order.
+cudaError_t run_col_split(rs_plan* p, const ColArgs& c, cudaStream_t s) {
+  const int n1y = p->ny / kFourN2;
+  auto ycols = [&](const float2* in, float2* out, int flags) {
+    ColArgs y{};
+    y.in = in; y.out = out; y.nx = p->nx; y.flags = flags; y.tw = p->tw_c1y;
+    y.pitch = static_cast<long long>(kFourN2) * p->nx; y.bstride = p->nx; y.batches = kFourN2;
+    y.tw4 = p->ny; y.tw4q = 1; y.tw4t = p->tw4y;
+    return launch_col_pass(n1y, y, s);
+  };
+  cudaError_t e = ycols(c.in, c.out, COL_FWD);
+  if (e != cudaSuccess) return e;
+  ColArgs m{};
+  m.in = c.out; m.out = c.out; m.nx = p->nx; m.tw = p->tw_256; m.tw2 = p->tw2_256;
+  m.ex = c.ex; m.ey = p->ey_s; m.ylim = c.ylim; m.kyi = p->kyi; m.scale = c.scale; m.flags = c.flags;
+  m.pitch = p->nx; m.bstride = static_cast<long long>(kFourN2) * p->nx; m.batches = n1y; m.ey_bstride = kFourN2;
+  e = launch_col_pass(kFourN2, m, s);
+  if (e != cudaSuccess) return e;
+  return ycols(c.out, c.out, COL_INV);
+}
+
 cudaError_t run_col(rs_plan* p, const ColArgs& ca, cudaStream_t s) {
+  if (p->split_cols && p->split_ok && ca.flags == (COL_FWD | COL_H | COL_SCALE | COL_INV) && ca.ey == p->ey)
+    return run_col_split(p, ca, s);
   ColArgs c = ca;
   c.tw2 = p->tw2_y;
   int w = 0, bh = 0;
@@ -315,7 +356,7 @@ int propagate_four(rs_plan* p, float2* u, float2* U, bool skip_fft, cudaStream_t
   auto xcols = [&](const float2* in, float2* out, int flags) {
     ColArgs c{};
     c.in = in; c.out = out; c.nx = kFourN2; c.flags = flags; c.tw = p->tw_c1x;
-    c.pitch = kFourN2; c.bstride = p->nx; c.batches = p->ny; c.tw4 = p->nx; c.tw4q = 0;
+    c.pitch = kFourN2; c.bstride = p->nx; c.batches = p->ny; c.tw4 = p->nx; c.tw4q = 0; c.tw4t = p->tw4x;
     return launch_col_pass(n1x, c, s);
   };
   auto xrows = [&](float2* f, int flags) {
@@ -327,7 +368,7 @@ int propagate_four(rs_plan* p, float2* u, float2* U, bool skip_fft, cudaStream_t
     ColArgs c{};
     c.in = f; c.out = f; c.nx = p->nx; c.flags = flags; c.tw = p->tw_c1y;
     c.pitch = static_cast<long long>(kFourN2) * p->nx; c.bstride = p->nx; c.batches = kFourN2;
-    c.tw4 = p->ny; c.tw4q = 1;
+    c.tw4 = p->ny; c.tw4q = 1; c.tw4t = p->tw4y;
     return launch_col_pass(n1y, c, s);
   };
   if (!skip_fft) {
@@ -596,11 +637,13 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   const size_t twy = fast ? std::max(stage_twiddle_len(ny), 1) : 0;
   const size_t tw2y = fast ? static_cast<size_t>(twiddles_2l_len(ny)) : 0;
   const size_t gx = (fast || four) ? 0 : nx, gy = (fast || four) ? 0 : ny;
-  const size_t n1x = four ? nx / kFourN2 : 0, n1y = four ? ny / kFourN2 : 0;
-  const size_t f256 = four ? std::max(stage_twiddle_len(kFourN2), 1) : 0;
-  const size_t f2l = four ? static_cast<size_t>(twiddles_2l_len(kFourN2)) : 0;
+  const bool split = fast && four_size(ny) && ny <= 16384;  // split columns available
+  const bool fy4 = four || split;                              // four-step y tables
+  const size_t n1x = four ? nx / kFourN2 : 0, n1y = fy4 ? ny / kFourN2 : 0;
+  const size_t f256 = fy4 ? std::max(stage_twiddle_len(kFourN2), 1) : 0;
+  const size_t f2l = fy4 ? static_cast<size_t>(twiddles_2l_len(kFourN2)) : 0;
   const size_t f1x = four ? std::max(stage_twiddle_len(static_cast<int>(n1x)), 1) : 0;
-  const size_t f1y = four ? std::max(stage_twiddle_len(static_cast<int>(n1y)), 1) : 0;
+  const size_t f1y = fy4 ? std::max(stage_twiddle_len(static_cast<int>(n1y)), 1) : 0;
   size_t bytes = 0;
   auto take = [&](size_t n) { const size_t at = bytes; bytes += (n + 15) & ~static_cast<size_t>(15); return at; };
   const size_t o_twx = take(sizeof(float4) * twx), o_twy = take(sizeof(float4) * twy);
@@ -612,7 +655,9 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   const size_t o_status = take(sizeof(int));
   const size_t o_f256 = take(sizeof(float4) * f256), o_f2l = take(sizeof(float4) * f2l);
   const size_t o_f1x = take(sizeof(float4) * f1x), o_f1y = take(sizeof(float4) * f1y);
-  const size_t o_kyi = take(four ? sizeof(int) * ny : 0);
+  const size_t o_kyi = take(fy4 ? sizeof(int) * ny : 0);
+  const size_t o_p4x = take(four ? sizeof(float4) * nx : 0), o_p4y = take(fy4 ? sizeof(float4) * ny : 0);
+  const size_t o_eys = take(split ? sizeof(float2) * ny : 0);
   e = cudaMalloc(&p->arena, bytes);
   if (e != cudaSuccess) { delete p; return fail(RS_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
   char* c = static_cast<char*>(p->arena);
@@ -620,15 +665,24 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
     p->tws_x = reinterpret_cast<float4*>(c + o_twx);
     p->tws_y = reinterpret_cast<float4*>(c + o_twy);
     if (tw2y) p->tw2_y = reinterpret_cast<float4*>(c + o_tw2y);
-  } else if (four) {
-    p->tw_256 = reinterpret_cast<float4*>(c + o_f256);
-    if (f2l) p->tw2_256 = reinterpret_cast<float4*>(c + o_f2l);
-    p->tw_c1x = reinterpret_cast<float4*>(c + o_f1x);
-    p->tw_c1y = reinterpret_cast<float4*>(c + o_f1y);
-    p->kyi = reinterpret_cast<int*>(c + o_kyi);
-  } else {
+  } else if (!four) {
     p->tw_x = reinterpret_cast<float2*>(c + o_gx);
     p->tw_y = reinterpret_cast<float2*>(c + o_gy);
+  }
+  if (fy4) {
+    p->tw_256 = reinterpret_cast<float4*>(c + o_f256);
+    if (f2l) p->tw2_256 = reinterpret_cast<float4*>(c + o_f2l);
+    p->tw_c1y = reinterpret_cast<float4*>(c + o_f1y);
+    p->tw4y = reinterpret_cast<float4*>(c + o_p4y);
+    p->kyi = reinterpret_cast<int*>(c + o_kyi);
+  }
+  if (four) {
+    p->tw_c1x = reinterpret_cast<float4*>(c + o_f1x);
+    p->tw4x = reinterpret_cast<float4*>(c + o_p4x);
+  }
+  if (split) {
+    p->split_ok = true;
+    p->ey_s = reinterpret_cast<float2*>(c + o_eys);
   }
   p->ex = reinterpret_cast<float2*>(c + o_ex);
   p->ey = reinterpret_cast<float2*>(c + o_ey);
@@ -648,15 +702,21 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
     p->pipe_rows = v == "1" || v == "rows";
     p->pipe_cols = v == "1" || v == "cols";
   }
-  if (four) {
-    e = launch_stage_twiddles(kFourN2, p->tw_256, 0);
-    if (e == cudaSuccess && p->tw2_256) e = launch_twiddles_2l(kFourN2, p->tw2_256, 0);
-    if (e == cudaSuccess) e = launch_stage_twiddles(static_cast<int>(n1x), p->tw_c1x, 0);
-    if (e == cudaSuccess) e = launch_stage_twiddles(static_cast<int>(n1y), p->tw_c1y, 0);
-  } else {
+  e = cudaSuccess;
+  if (!four) {
     e = fast ? launch_stage_twiddles(nx, p->tws_x, 0) : launch_twiddles(p->tw_x, nx, 0);
     if (e == cudaSuccess) e = fast ? launch_stage_twiddles(ny, p->tws_y, 0) : launch_twiddles(p->tw_y, ny, 0);
     if (e == cudaSuccess && p->tw2_y) e = launch_twiddles_2l(ny, p->tw2_y, 0);
+  }
+  if (split || four) {
+    if (e == cudaSuccess) e = launch_stage_twiddles(kFourN2, p->tw_256, 0);
+    if (e == cudaSuccess && p->tw2_256) e = launch_twiddles_2l(kFourN2, p->tw2_256, 0);
+    if (e == cudaSuccess) e = launch_stage_twiddles(static_cast<int>(n1y), p->tw_c1y, 0);
+    if (e == cudaSuccess) e = launch_power_twiddles(ny, p->tw4y, 0);
+  }
+  if (four) {
+    if (e == cudaSuccess) e = launch_stage_twiddles(static_cast<int>(n1x), p->tw_c1x, 0);
+    if (e == cudaSuccess) e = launch_power_twiddles(nx, p->tw4x, 0);
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(p->status, 0, sizeof(int), 0);
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);
@@ -696,11 +756,12 @@ int rs_plan_set_pipeline(rs_plan* p, int mask) {
 
 int rs_plan_set_schedule(rs_plan* p, int mask) {
   RS_TRY(check_plan(p));
-  if (mask & ~(RS_SCHED_PIPE_ROWS | RS_SCHED_PIPE_COLS | RS_SCHED_ROW_GENERAL))
+  if (mask & ~(RS_SCHED_PIPE_ROWS | RS_SCHED_PIPE_COLS | RS_SCHED_ROW_GENERAL | RS_SCHED_SPLIT_COLS))
     return fail(RS_EINVAL, "unknown schedule bits 0x%x", mask);
   p->pipe_rows = (mask & RS_SCHED_PIPE_ROWS) != 0;
   p->pipe_cols = (mask & RS_SCHED_PIPE_COLS) != 0;
   p->row_vox = (mask & RS_SCHED_ROW_GENERAL) == 0;
+  p->split_cols = (mask & RS_SCHED_SPLIT_COLS) != 0;
   return RS_OK;
 }
 
@@ -708,7 +769,7 @@ int rs_plan_get_schedule(const rs_plan* p, int* mask) {
   RS_TRY(check_plan(p));
   if (!mask) return fail(RS_EINVAL, "mask is NULL");
   *mask = (p->pipe_rows ? RS_SCHED_PIPE_ROWS : 0) | (p->pipe_cols ? RS_SCHED_PIPE_COLS : 0) |
-          (p->row_vox ? 0 : RS_SCHED_ROW_GENERAL);
+          (p->row_vox ? 0 : RS_SCHED_ROW_GENERAL) | (p->split_cols ? RS_SCHED_SPLIT_COLS : 0);
   return RS_OK;
 }
 
@@ -721,7 +782,8 @@ int rs_plan_schedules(const rs_plan* p, int* masks, int cap, int* count) {
   const bool rows_pipe = p->fast && row_pipe_ok(p->nx);
   const bool cols_pipe = p->fast && col_pipe_box(p->ny, &w, &bh);
   int n = 0;
-  for (int m = 0; m < 8; ++m) {
+  for (int m = 0; m < 16; ++m) {
+    if ((m & RS_SCHED_SPLIT_COLS) && !p->split_ok) continue;
     if ((m & RS_SCHED_PIPE_ROWS) && !rows_pipe) continue;
     if ((m & RS_SCHED_PIPE_COLS) && !cols_pipe) continue;
     if ((m & RS_SCHED_ROW_GENERAL) && (!p->fast || (m & RS_SCHED_PIPE_ROWS))) continue;

@@ -23,6 +23,19 @@ cudaError_t launch_col_pass(int ny, const ColArgs& a, cudaStream_t s) {
   return is_pow2(ny) ? launch_col_pass_pow2(ny, a, s) : launch_col_pass_pow3(ny, a, s);
 }
 
+__global__ void power_twiddles_kernel(float4* tw, int n) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m < n) tw[m] = twiddle_fp64(m, n);
+}
+
+cudaError_t launch_power_twiddles(int n, float4* tw, cudaStream_t s) {
+  if (!is_pow2(n)) return cudaErrorInvalidValue;
+  power_twiddles_kernel<<<(n + 255) / 256, 256, 0, s>>>(tw, n);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) note_launch();
+  return e;
+}
+
 cudaError_t launch_stage_twiddles(int n, float4* tw, cudaStream_t s) {
   return is_pow2(n) ? launch_stage_twiddles_pow2(n, tw, s) : launch_stage_twiddles_pow3(n, tw, s);
 }

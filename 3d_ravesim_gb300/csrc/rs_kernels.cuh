@@ -106,9 +106,11 @@ struct ColArgs {
   const int* kyi;        // signed y-frequency index per storage row (null: natural order)
   // Four-step twiddle W_L^{p*q} (W_L = exp(-2 pi i/L)), p = the transform position of the value,
   // q = the column (tw4q = 0) or blockIdx.y (tw4q = 1): multiplied after a forward transform,
-  // conjugated before an inverse one. L = tw4, a power of two <= 32768; 0 = none.
+  // conjugated before an inverse one. L = tw4, a power of two <= 32768; 0 = none. tw4t holds
+  // W_L^m for m < L, compensated (hi, lo) like the stage tables.
   int tw4;
   int tw4q;
+  const float4* tw4t;
 };
 
 // ----------------------------------------------------------------------------- physics
@@ -651,16 +653,12 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T, (W * FftPlan<N>::T <= 512 ?
     for (int e = 0; e < E; ++e) v[e] = in[static_cast<size_t>(col_exit_pos<N, L2>(t, e)) * pitch + x];
   }
   if (a.tw4) {
-    // registers hold transform positions fy (forward exit == inverse entry mapping); the angle
-    // -2 pi (fy*q mod L)/L is exact in float (L <= 2^15), so sincospif gets an exact argument
+    // registers hold transform positions fy (forward exit == inverse entry mapping)
     const int q = a.tw4q ? static_cast<int>(blockIdx.y) : x;
-    const float inv_half = 2.0f / static_cast<float>(a.tw4);
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const int pq = (col_exit_pos<N, L2>(t, e) * q) & (a.tw4 - 1);
-      float sn, cs;
-      sincospif(-static_cast<float>(pq) * inv_half, &sn, &cs);
-      v[e] = cmul(v[e], make_float2(cs, (flags & COL_FWD) ? sn : -sn));
+      const float4 w = __ldg(&a.tw4t[(col_exit_pos<N, L2>(t, e) * q) & (a.tw4 - 1)]);
+      v[e] = (flags & COL_FWD) ? cmul_tw(v[e], w) : cmulc_tw(v[e], w);
     }
   }
 
@@ -716,6 +714,8 @@ cudaError_t launch_row_pass(int nx, const RowArgs& a, cudaStream_t s, bool vox =
 cudaError_t launch_row_adjoint(int nx, const RowArgs& a, cudaStream_t s);
 // Compensated stage-major twiddle tables of the fused passes for length n (fast sizes only).
 cudaError_t launch_stage_twiddles(int n, float4* tw, cudaStream_t s);
+// W_n^m for m < n, compensated, n a power of two (the four-step twiddle table).
+cudaError_t launch_power_twiddles(int n, float4* tw, cudaStream_t s);
 int stage_twiddle_len(int n);
 // Two-level column-transform table of length n (0 when n has none) and its builder.
 int twiddles_2l_len(int n);

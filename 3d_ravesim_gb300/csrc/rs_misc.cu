@@ -44,10 +44,10 @@ __device__ __forceinline__ int storage_freq(int i, int n, int n2) {
 
 __global__ void prop_tables_kernel(const PropTabArgs a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < a.nx) {
+  if (i < a.nx && (a.ex || a.ylim)) {
     const int mx = signed_index(storage_freq(i, a.nx, a.n2x), a.nx);
     const double kx2 = kfreq2_abs(mx < 0 ? -mx : mx, a.nx, a.dx);
-    if (a.with_h) {
+    if (a.with_h && a.ex) {
       double s, c;
       sincos(__dmul_rn(a.ps, kx2), &s, &c);
       a.ex[i] = make_float2(static_cast<float>(c), static_cast<float>(s));
@@ -63,10 +63,10 @@ __global__ void prop_tables_kernel(const PropTabArgs a) {
       }
       lim = lo;
     }
-    a.ylim[i] = lim;
+    if (a.ylim) a.ylim[i] = lim;
   }
   if (a.kyi && i < a.ny) a.kyi[i] = signed_index(storage_freq(i, a.ny, a.n2y), a.ny);
-  if (a.with_h && i < a.ny) {
+  if (a.with_h && a.ey && i < a.ny) {
     const int my = signed_index(storage_freq(i, a.ny, a.n2y), a.ny);
     const double ky2 = kfreq2_abs(my < 0 ? -my : my, a.ny, a.dy);
     double s, c, gs, gc;

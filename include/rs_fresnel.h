@@ -223,12 +223,18 @@ int rs_plan_set_pipeline(rs_plan* plan, int mask);
  *   RS_SCHED_PIPE_COLS   column passes as the persistent tensor-copy pipeline (strips of columns
  *                        loaded by TMA boxes, NB buffers) instead of one block per strip;
  *   RS_SCHED_ROW_GENERAL the multislice rows run the general row kernel instead of the
- *                        voxel-only specialisation.
+ *                        voxel-only specialisation;
+ *   RS_SCHED_SPLIT_COLS  (ny = n1*256 in [4096, 16384]) the column pass of a multislice step runs
+ *                        as three shorter passes: length-n1 transforms with the W_ny twiddle,
+ *                        length-256 transform / H / inverse, length-n1 inverse. Rounding differs
+ *                        from the single pass at the FP32 level (the other bits reproduce it
+ *                        exactly).
  * rs_plan_schedules lists the masks that are distinct for the plan's sizes (it writes at most
  * `cap` of them and the total to *count). No reference function: big-wave has one FFT schedule. */
 #define RS_SCHED_PIPE_ROWS 1
 #define RS_SCHED_PIPE_COLS 2
 #define RS_SCHED_ROW_GENERAL 4
+#define RS_SCHED_SPLIT_COLS 8
 int rs_plan_set_schedule(rs_plan* plan, int mask);
 int rs_plan_get_schedule(const rs_plan* plan, int* mask);
 int rs_plan_schedules(const rs_plan* plan, int* masks, int cap, int* count);

@@ -17,7 +17,8 @@ def at(monkeypatch, tmp_path):
 
 def test_schedule_lists(rs, cuda):
     lib = rs._lib
-    assert lib.plan_for(4096, 4096, cuda).schedules() == [0, 1, 2, 3, 4, 6]
+    assert lib.plan_for(4096, 4096, cuda).schedules() == [0, 1, 2, 3, 4, 6, 8, 9, 10, 11, 12, 14]
+    assert lib.plan_for(2048, 2048, cuda).schedules() == [0, 1, 2, 3, 4, 6]  # no split below 4096
     assert lib.plan_for(8192, 64, cuda).schedules() == [0, 1, 4]
     assert lib.plan_for(72, 40, cuda).schedules() == [0]  # direct-DFT sizes have one schedule
     p = lib.plan_for(1024, 1024, cuda)
@@ -26,7 +27,7 @@ def test_schedule_lists(rs, cuda):
     assert p.schedule() == 6
     p.set_schedule(old)
     with pytest.raises(Exception):
-        p.set_schedule(8)
+        p.set_schedule(16)
 
 
 @pytest.mark.parametrize("n", [1024, 1536])

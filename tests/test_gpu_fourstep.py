@@ -115,3 +115,75 @@ def test_32768_round_trip_and_parseval(rs, cuda):
     assert img.shape == (512, 512) and np.isfinite(img).all()
     del u, U, u0
     torch.cuda.empty_cache()
+
+
+def shell_sample(rs, nz, ny_v, nx_v, pitch, seed=0):
+    zz = (np.arange(nz) - (nz - 1) / 2.0)[:, None, None] * pitch
+    yy = (np.arange(ny_v) - ny_v / 2.0)[None, :, None] * pitch
+    xx = (np.arange(nx_v) - nx_v / 2.0)[None, None, :] * pitch
+    r = np.sqrt(xx ** 2 + yy ** 2 + zz ** 2)
+    rmax = 0.45 * min(ny_v, nx_v) * pitch
+    grid = ((r <= rmax) & (r >= 0.8 * rmax)).astype(np.uint32)
+    s = rs.Sample(z_start=0.1, pixel_size_x=pitch, pixel_size_z=2e-6, grid=grid, materials=[rs.Material("A", 1.0)],
+                  x_positions=np.array([0.0]), pixel_size_y=pitch, y_positions=np.array([0.0]))
+    s.db_list = np.array([0.0, 2.5e-7 + 1.5e-10j])
+    return s
+
+
+@pytest.mark.parametrize("nx,ny,slices", [(1024, 4096, 6)])
+def test_split_columns_vs_fp64_oracle(rs, cuda, oracle, nx, ny, slices):
+    """Sample.apply with the three-pass columns (RS_SCHED_SPLIT_COLS) against big-wave's FP64
+    restatement, and against the single column pass."""
+    dx = 0.25e-6
+    wl = rs.convert_energy_wavelength(20000.0)
+    p = rs.SimParams(N=nx * ny, nx=nx, ny=ny, dx=dx, dy=dx, z_detector=1.0, detector_size=nx * dx,
+                     detector_pixel_size_x=dx, detector_pixel_size_y=dx, wl=wl, chunk_size=nx)
+    s = shell_sample(rs, slices, ny + 2, nx + 2, dx)
+    f = 0.45 / dx
+    plan = rs._lib.plan_for(nx, ny, cuda)
+    assert 8 in plan.schedules()
+    g = torch.Generator(device="cpu").manual_seed(2)
+    u0 = torch.polar(torch.ones(nx * ny), torch.rand(nx * ny, generator=g) * 0.3).to(torch.complex64)
+    out = {}
+    old = plan.schedule()
+    try:
+        for mask in (old & ~8, old | 8):
+            plan.set_schedule(mask)
+            u = rs.GpuVector(u0.clone().to(cuda))
+            U = rs.GpuVector.zeros(nx * ny, cuda)
+            s.apply(u, U, p, f, 0, None)
+            out[mask] = u.to_numpy().reshape(ny, nx)
+    finally:
+        plan.set_schedule(old)
+    single, split = out[old & ~8], out[old | 8]
+    assert rel_l2(split, single) < 5e-6
+    ref, _ = oracle.sample_apply_2d(u0.numpy().astype(np.complex128).reshape(ny, nx), np.asarray(s.grid), s.db_list,
+                                    dx, dx, wl, f, s.pixel_size_x, s.pixel_size_y, s.pixel_size_z)
+    assert rel_l2(split, ref) < 1e-5
+    assert rel_l2(single, ref) < 1e-5
+
+
+def test_split_columns_16384(rs, cuda):
+    """The 16384-point columns of the large-field case: three-pass columns against the single
+    per-block column pass over a few voxel slices."""
+    nx, ny, slices = 512, 16384, 4
+    dx = 50e-9
+    wl = rs.convert_energy_wavelength(30000.0)
+    p = rs.SimParams(N=nx * ny, nx=nx, ny=ny, dx=dx, dy=dx, z_detector=1.0, detector_size=nx * dx,
+                     detector_pixel_size_x=dx, detector_pixel_size_y=dx, wl=wl, chunk_size=nx)
+    s = shell_sample(rs, slices, ny + 2, nx + 2, dx)
+    plan = rs._lib.plan_for(nx, ny, cuda)
+    g = torch.Generator(device="cpu").manual_seed(4)
+    u0 = torch.polar(torch.ones(nx * ny), torch.rand(nx * ny, generator=g) * 0.3).to(torch.complex64)
+    out = {}
+    old = plan.schedule()
+    try:
+        for mask in (0, 8):
+            plan.set_schedule(mask)
+            u = rs.GpuVector(u0.clone().to(cuda))
+            U = rs.GpuVector.zeros(nx * ny, cuda)
+            s.apply(u, U, p, 0.45 / dx, 0, None)
+            out[mask] = u.to_numpy()
+    finally:
+        plan.set_schedule(old)
+    assert rel_l2(out[8], out[0]) < 5e-6
