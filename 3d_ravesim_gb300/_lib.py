@@ -176,10 +176,10 @@ class Plan:
 
     def schedules(self) -> list[int]:
         """The schedule masks that are distinct for this plan's sizes."""
-        buf = (c_int * 8)()
+        buf = (c_int * 16)()
         n = c_int(0)
-        check(lib().rs_plan_schedules(self.handle, buf, 8, ctypes.byref(n)), "rs_plan_schedules")
-        return [buf[i] for i in range(min(n.value, 8))]
+        check(lib().rs_plan_schedules(self.handle, buf, 16, ctypes.byref(n)), "rs_plan_schedules")
+        return [buf[i] for i in range(min(n.value, 16))]
 
     def status(self) -> int:
         """Synchronise and return the device status word (0 = no bounded wait gave up)."""
