@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=4096, help="field size (default 4096)")
     ap.add_argument("--slices", type=int, default=512)
+    ap.add_argument("--schedule", default="auto",
+                    help="pass schedule of the field's plan: 'auto' (tuned at start-up) or a mask (1 pipelined "
+                         "rows, 2 pipelined columns, 4 general row kernel, 8 split columns)")
     ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/cpu/accuracy legs")
     ap.add_argument("--workload", default="talbot", choices=["talbot", "capsule"],
                     help="talbot: the 4096^2 Talbot-Lau benchmark (default); capsule: the 16384^2 "
@@ -494,7 +497,10 @@ def run_ours(args):
     # pass schedule of the field's plan: every distinct schedule timed on a few seeded voxel
     # slices of this size, the fastest kept (nothing is read from or written to the cache file)
     autotune = importlib.import_module("3d_ravesim_gb300.autotune")
-    tuned = autotune.tune_multislice(w.params.nx, w.params.ny, device, store=False)
+    if args.schedule == "auto":
+        tuned = autotune.tune_multislice(w.params.nx, w.params.ny, device, store=False)
+    else:
+        tuned = autotune.Choice(int(args.schedule), {}, 0, {})
     rs._lib.plan_for(w.params.nx, w.params.ny, device).set_schedule(tuned.mask)
     stream = torch.cuda.current_stream(device)
     flush = l2_flush_buffer(torch, device)
@@ -577,8 +583,8 @@ def run_ours(args):
             "schedule": {"mask": tuned.mask, "passes": schedule_name(tuned.mask),
                          "tuned_ms_per_schedule": {schedule_name(m): round(t, 3)
                                                    for m, t in sorted(tuned.timings_ms.items())},
-                         "tuned_on": f"{tuned.slices} seeded voxel slices at {n}^2",
-                         "max_rel_diff_between_schedules": max(tuned.rel_diff.values())}}
+                         "tuned_on": f"{tuned.slices} seeded voxel slices at {n}^2" if tuned.slices else "given",
+                         "max_rel_diff_between_schedules": max(tuned.rel_diff.values(), default=None)}}
 
     if rank == 0 and not args.no_extras:
         # e2e: every step copies its voxel grids in from pinned host memory and the detector image
