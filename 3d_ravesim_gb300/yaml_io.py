@@ -1,12 +1,13 @@
-"""Block-style YAML for the run-directory metadata files (detector_metadata.yaml,
-source_geometry.yaml, history_metadata.yaml).
+"""Block-style YAML for big-wave's simulation directories: the metadata files a run writes
+(detector_metadata.yaml, source_geometry.yaml, history_metadata.yaml) and the prepared
+configuration it reads (config.yaml, computed.yaml, subconfig.yaml).
 
 big-wave writes them with ruamel's round-trip dumper, mapping indent 2, sequence indent 4, dash
 offset 2 (big-wave/config.py:516-520). Neither ruamel nor PyYAML is a dependency here, so this
 module writes that layout for the value types the metadata holds (mappings, sequences, str,
 int, float, bool, None) and reads the same subset back (YAML 1.2 core-schema scalars: null/~,
 true/false, decimal ints, floats incl. .inf/.nan, single- and double-quoted strings, empty
-flow collections and flow sequences of scalars).
+flow collections and flow sequences of scalars; node tags such as !!python/tuple are skipped).
 """
 from __future__ import annotations
 
@@ -107,6 +108,7 @@ def _parse_scalar(s: str) -> Any:
         if not s.endswith('"') or len(s) < 2:
             raise ValueError(f"unterminated quoted scalar {s!r}")
         return bytes(s[1:-1], "utf-8").decode("unicode_escape")
+    s = _strip_tag(s)
     if s in ("", "~", "null", "Null", "NULL"):
         return None
     if s in ("true", "True", "TRUE"):
@@ -141,6 +143,14 @@ def _strip_comment(line: str) -> str:
     return line.rstrip()
 
 
+def _strip_tag(text: str) -> str:
+    """Drop a leading node tag (!!python/tuple, !!float, ...): the values are read by their text."""
+    if text.startswith("!"):
+        parts = text.split(None, 1)
+        return parts[1] if len(parts) > 1 else ""
+    return text
+
+
 def _split_key(text: str):
     """'key: value' -> (key, value) honouring a quoted key; None if text is not a mapping entry."""
     if text.startswith(("'", '"')):
@@ -160,7 +170,7 @@ def _split_key(text: str):
     m = re.match(r"^([^:#]+?):(\s|$)(.*)$", text)
     if not m:
         return None
-    return _parse_scalar(m.group(1)), m.group(3).strip()
+    return _parse_scalar(m.group(1)), _strip_tag(m.group(3).strip())
 
 
 def loads(text: str) -> Any:
@@ -181,7 +191,7 @@ def loads(text: str) -> Any:
         if txt.startswith("- ") or txt == "-":
             seq = []
             while pos < len(lines) and lines[pos][0] == ind and (lines[pos][1].startswith("- ") or lines[pos][1] == "-"):
-                item = lines[pos][1][1:].strip()
+                item = _strip_tag(lines[pos][1][1:].strip())
                 if not item:
                     pos += 1
                     seq.append(block(lines[pos][0]) if pos < len(lines) and lines[pos][0] > ind else None)

@@ -114,3 +114,21 @@ def test_run_single_source_writes_run_directory(rs, cuda, tmp_path):
     assert hmeta["frames"] == len(g["run_history_z"]) and hmeta["storage"] == "npy"
     manifest = (tmp_path / "ck" / "00000003" / "manifest.json").read_text()
     assert '"status": "complete"' in manifest
+
+
+def test_run_single_simulation_from_prepared_directory(rs, cuda, tmp_path):
+    """multisim.run_single_simulation on a directory in setup_simulation's layout gives
+    big-wave's recorded image and history."""
+    from prepared_dir import write_prepared_dir
+    g = np.load(GOLDEN)
+    ms = importlib.import_module("3d_ravesim_gb300.multisim")
+    yio = importlib.import_module("3d_ravesim_gb300.yaml_io")
+    sim = write_prepared_dir(yio, tmp_path, g)
+    outs = ms.run_single_simulation(sim, 0, tmp_path / "scratch", history_dz=float(g["run_params"][4]), device=cuda)
+    sub = sim / "00000000"
+    det = np.load(sub / "detected.npy")
+    np.testing.assert_array_equal(det[0], outs[0])
+    assert rel_l2(det[0], g["run_out"]) < 2e-5
+    assert rel_l2(np.load(sub / "history.npy"), g["run_history"]) < 2e-5
+    meta = yio.load(sub / "detector_metadata.yaml")
+    assert meta["source_geometry"]["y_origin"] == "explicit" and meta["phase_steps"] == 1
