@@ -84,8 +84,7 @@ struct rs_plan {
   float4* tw2_256 = nullptr;  // two-level table of the length-256 column transform
   float4* tw_c1x = nullptr;   // stage-major tables of the length-n1 column transforms
   float4* tw_c1y = nullptr;
-  float4* tw4x = nullptr;     // W_n^m tables of the fused four-step twiddles (compensated)
-  float4* tw4y = nullptr;
+  float4* tw4y = nullptr;     // W_ny^m for the fused y twiddles (compensated; the x ones use sincospif)
   int* kyi = nullptr;         // signed y-frequency index per storage row
   // Split columns (fast plans with ny = n1 * 256 in [4096, 16384]): the fused column pass of a
   // multislice step as three passes (length-n1 forward with W_ny, length-256 forward / H /
@@ -356,7 +355,7 @@ int propagate_four(rs_plan* p, float2* u, float2* U, bool skip_fft, cudaStream_t
   auto xcols = [&](const float2* in, float2* out, int flags) {
     ColArgs c{};
     c.in = in; c.out = out; c.nx = kFourN2; c.flags = flags; c.tw = p->tw_c1x;
-    c.pitch = kFourN2; c.bstride = p->nx; c.batches = p->ny; c.tw4 = p->nx; c.tw4q = 0; c.tw4t = p->tw4x;
+    c.pitch = kFourN2; c.bstride = p->nx; c.batches = p->ny; c.tw4 = p->nx; c.tw4q = 0;  // sincospif twiddles
     return launch_col_pass(n1x, c, s);
   };
   auto xrows = [&](float2* f, int flags) {
@@ -656,7 +655,7 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   const size_t o_f256 = take(sizeof(float4) * f256), o_f2l = take(sizeof(float4) * f2l);
   const size_t o_f1x = take(sizeof(float4) * f1x), o_f1y = take(sizeof(float4) * f1y);
   const size_t o_kyi = take(fy4 ? sizeof(int) * ny : 0);
-  const size_t o_p4x = take(four ? sizeof(float4) * nx : 0), o_p4y = take(fy4 ? sizeof(float4) * ny : 0);
+  const size_t o_p4y = take(fy4 ? sizeof(float4) * ny : 0);
   const size_t o_eys = take(split ? sizeof(float2) * ny : 0);
   e = cudaMalloc(&p->arena, bytes);
   if (e != cudaSuccess) { delete p; return fail(RS_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
@@ -678,7 +677,6 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   }
   if (four) {
     p->tw_c1x = reinterpret_cast<float4*>(c + o_f1x);
-    p->tw4x = reinterpret_cast<float4*>(c + o_p4x);
   }
   if (split) {
     p->split_ok = true;
@@ -716,7 +714,6 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   }
   if (four) {
     if (e == cudaSuccess) e = launch_stage_twiddles(static_cast<int>(n1x), p->tw_c1x, 0);
-    if (e == cudaSuccess) e = launch_power_twiddles(nx, p->tw4x, 0);
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(p->status, 0, sizeof(int), 0);
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);

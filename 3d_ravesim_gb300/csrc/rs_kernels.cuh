@@ -107,7 +107,7 @@ struct ColArgs {
   // Four-step twiddle W_L^{p*q} (W_L = exp(-2 pi i/L)), p = the transform position of the value,
   // q = the column (tw4q = 0) or blockIdx.y (tw4q = 1): multiplied after a forward transform,
   // conjugated before an inverse one. L = tw4, a power of two <= 32768; 0 = none. tw4t holds
-  // W_L^m for m < L, compensated (hi, lo) like the stage tables.
+  // W_L^m for m < L, compensated (hi, lo) like the stage tables; null: computed with sincospif.
   int tw4;
   int tw4q;
   const float4* tw4t;
@@ -655,10 +655,24 @@ __global__ void __launch_bounds__(W * FftPlan<N>::T, (W * FftPlan<N>::T <= 512 ?
   if (a.tw4) {
     // registers hold transform positions fy (forward exit == inverse entry mapping)
     const int q = a.tw4q ? static_cast<int>(blockIdx.y) : x;
+    if (a.tw4t) {
+      // compensated table; with q = blockIdx.y every column of the strip reads the same entry
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const float4 w = __ldg(&a.tw4t[(col_exit_pos<N, L2>(t, e) * q) & (a.tw4 - 1)]);
-      v[e] = (flags & COL_FWD) ? cmul_tw(v[e], w) : cmulc_tw(v[e], w);
+      for (int e = 0; e < E; ++e) {
+        const float4 w = __ldg(&a.tw4t[(col_exit_pos<N, L2>(t, e) * q) & (a.tw4 - 1)]);
+        v[e] = (flags & COL_FWD) ? cmul_tw(v[e], w) : cmulc_tw(v[e], w);
+      }
+    } else {
+      // per-column q would scatter table reads over the warp: sincospif of the exact reduced
+      // angle -2 (fy*q mod L)/L (exact in float for L <= 2^15) instead
+      const float inv_half = 2.0f / static_cast<float>(a.tw4);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        const int pq = (col_exit_pos<N, L2>(t, e) * q) & (a.tw4 - 1);
+        float sn, cs;
+        sincospif(-static_cast<float>(pq) * inv_half, &sn, &cs);
+        v[e] = cmul(v[e], make_float2(cs, (flags & COL_FWD) ? sn : -sn));
+      }
     }
   }
 
