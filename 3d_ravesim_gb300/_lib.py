@@ -58,6 +58,8 @@ _SIGS = {
                                     c_double, _P], c_int),
     "rs_multislice_voxel": ([_P, _P, _P, _P, c_int, _P, c_int, ctypes.POINTER(VoxelGeom), c_double,
                              c_double, c_double, c_double, _DP, _DP, c_int, c_int, _P], c_int),
+    "rs_multislice_voxel_stacked": ([_P, c_int, _P, _P, _P, c_int, _P, c_int, ctypes.POINTER(VoxelGeom),
+                                     c_double, c_double, c_double, c_double, _DP, _DP, c_int, c_int, _P], c_int),
     "rs_multislice_plasma": ([_P, _P, _P, _P, _P, _P, _P, c_int, ctypes.POINTER(PlasmaConsts),
                               ctypes.POINTER(VoxelGeom), c_double, c_double, c_double, c_double,
                               _DP, _DP, c_int, c_int, _P], c_int),

@@ -274,12 +274,15 @@ cudaError_t run_col_split(rs_plan* p, const ColArgs& c, cudaStream_t s) {
 }
 
 cudaError_t run_col(rs_plan* p, const ColArgs& ca, cudaStream_t s) {
-  if (p->split_cols && p->split_ok && ca.flags == (COL_FWD | COL_H | COL_SCALE | COL_INV) && ca.ey == p->ey)
+  const bool stacked = ca.batches > 1;  // stacked fields: the per-block kernel's batches
+  if (!stacked && p->split_cols && p->split_ok && ca.flags == (COL_FWD | COL_H | COL_SCALE | COL_INV) &&
+      ca.ey == p->ey)
     return run_col_split(p, ca, s);
   ColArgs c = ca;
   c.tw2 = p->tw2_y;
   int w = 0, bh = 0;
-  if (p->pipe_cols && col_pipe_box(p->ny, &w, &bh) && aligned16(c.in) && aligned16(c.out) && tensor_map_encoder()) {
+  if (!stacked && p->pipe_cols && col_pipe_box(p->ny, &w, &bh) && aligned16(c.in) && aligned16(c.out) &&
+      tensor_map_encoder()) {
     // Copy the input map before the output lookup: encoding the output may recycle its slot.
     const CUtensorMap* mi = field_map(p, c.in, w, bh);
     if (mi) {
@@ -401,6 +404,7 @@ int generic_slice(rs_plan* p, float2* u, float2* U, const VoxelArgs* vox, const 
 struct SliceSource {
   // exactly one of vox / pl is used
   bool plasma = false;
+  int batch = 1;               // stacked fields (same size, energy and sample; consecutive in u and U)
   const char* grid = nullptr;  // voxel ids
   const float2* dbv = nullptr; // or (delta, beta) per voxel
   int grid_signed = 0;
@@ -426,6 +430,10 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
   if (!slice_dz) return fail(RS_EINVAL, "slice_dz is NULL");
   if (!finite_pos(wl)) return fail(RS_EINVAL, "wavelength must be positive");
   if (s0 == s1) return RS_OK;
+  if (src.batch < 1) return fail(RS_EINVAL, "batch must be >= 1, got %d", src.batch);
+  if (src.batch > 1 && !p->fast) return fail(RS_EUNSUPPORTED, "stacked fields need a fused-kernel plan");
+  if (src.batch > 1 && static_cast<long long>(p->ny) * src.batch > (1LL << 30))
+    return fail(RS_EINVAL, "batch %d x %d rows is too many", src.batch, p->ny);
   const size_t plane = static_cast<size_t>(g->ny_v) * g->nx_v;
   const float a = static_cast<float>(g->pixel_size_z / wl);
   const float inv_n = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
@@ -468,7 +476,8 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
     }
     if (p->fast) {
       RowArgs r{};
-      r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tws_x; r.ax = axis_tab(p);
+      r.in = u; r.out = u; r.ny = p->ny * src.batch; r.tw = p->tws_x; r.ax = axis_tab(p);
+      r.axis_rows = src.batch > 1 ? p->ny : 0;
       r.flags = (z == s0 ? 0 : ROW_INV) | ROW_FWD | (src.plasma ? ROW_TPLASMA : ROW_TVOX);
       if (src.store) {
         r.flags |= ROW_STORE_U;
@@ -483,6 +492,10 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       c.in = u; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tws_y;
       c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
       c.flags = COL_FWD | COL_H | COL_SCALE | COL_INV | (z == s1 - 1 ? COL_SPEC : 0);
+      if (src.batch > 1) {
+        c.batches = src.batch;
+        c.bstride = static_cast<long long>(p->nx) * p->ny;
+      }
       const int ec = prof_begin(p, 1, s);
       RS_CK(run_col(p, c, s));
       prof_end(p, ec, s);
@@ -492,7 +505,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
   }
   if (p->fast) {
     RowArgs r{};
-    r.in = u; r.out = u; r.ny = p->ny; r.tw = p->tws_x; r.flags = ROW_INV;
+    r.in = u; r.out = u; r.ny = p->ny * src.batch; r.tw = p->tws_x; r.flags = ROW_INV;
     RS_CK(run_row(p, r, s));
   }
   return RS_OK;
@@ -992,6 +1005,23 @@ int rs_multislice_voxel(rs_plan* p, void* u, void* U, const void* grid, int grid
   src.grid_signed = grid_signed;
   src.db = reinterpret_cast<const float2*>(db);
   src.n_db = n_db;
+  return multislice(p, static_cast<float2*>(u), static_cast<float2*>(U), src, geom, dx, dy, wl, cutoff,
+                    slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
+}
+
+int rs_multislice_voxel_stacked(rs_plan* p, int batch, void* u, void* U, const void* grid, int grid_signed,
+                                const float* db, int n_db, const rs_voxel_geom* geom, double dx, double dy,
+                                double wl, double cutoff, const double* slice_dz, const double* coord_scale,
+                                int slice_begin, int slice_end, void* stream) {
+  RS_TRY(check_plan_std(p, "rs_multislice_voxel_stacked"));
+  if (!grid || !db) return fail(RS_EINVAL, "grid and db must be device pointers");
+  if (n_db < 1) return fail(RS_EINVAL, "n_db must be >= 1");
+  SliceSource src;
+  src.grid = static_cast<const char*>(grid);
+  src.grid_signed = grid_signed;
+  src.db = reinterpret_cast<const float2*>(db);
+  src.n_db = n_db;
+  src.batch = batch;
   return multislice(p, static_cast<float2*>(u), static_cast<float2*>(U), src, geom, dx, dy, wl, cutoff,
                     slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
 }

@@ -84,6 +84,7 @@ struct RowArgs {
   PointSrcArgs ps;
   float2* aux;           // ROW_STORE_U: the fields entering the slice; adjoint: read from here
   float* grad;           // adjoint: dL/d(delta, beta) of the slice, float pairs per voxel
+  int axis_rows;         // stacked fields: rows per field (the y tables repeat); 0 = ny
 };
 
 struct ColArgs {
@@ -406,8 +407,9 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   uint32_t* pf = reinterpret_cast<uint32_t*>(smem + ROWS * P::S) + lr * RowGeom<N, ROWS>::PF_WORDS;
   if (tmode) {
     if (valid) {
-      yi = __ldg(&a.ax.yi[row]);
-      if (yi >= 0) fy = __ldg(&a.ax.yf[row]);
+      const int ar = a.axis_rows ? row % a.axis_rows : row;  // row of its own field
+      yi = __ldg(&a.ax.yi[ar]);
+      if (yi >= 0) fy = __ldg(&a.ax.yf[ar]);
     }
     if constexpr (RowGeom<N, ROWS>::PF) {
       pf_on = prefetch_words(vox, a.vox, a.pl) <= RowGeom<N, ROWS>::PF_WORDS;
@@ -531,8 +533,9 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   int yi = -1;
   float fy = 0.0f;
   if (valid) {
-    yi = __ldg(&a.ax.yi[row]);
-    if (yi >= 0) fy = __ldg(&a.ax.yf[row]);
+    const int ar = a.axis_rows ? row % a.axis_rows : row;  // row of its own field
+    yi = __ldg(&a.ax.yi[ar]);
+    if (yi >= 0) fy = __ldg(&a.ax.yf[ar]);
   }
   if (flags & ROW_INV) {
 #pragma unroll

@@ -224,8 +224,9 @@ __global__ void __launch_bounds__(RowPipeGeom<N>::THREADS, RowPipeGeom<N>::MINB)
       int yi = -1;
       float fy = 0.0f;
       if (valid) {
-        yi = __ldg(&a.ax.yi[row]);
-        if (yi >= 0) fy = __ldg(&a.ax.yf[row]);
+        const int ar = a.axis_rows ? row % a.axis_rows : row;  // row of its own field
+        yi = __ldg(&a.ax.yi[ar]);
+        if (yi >= 0) fy = __ldg(&a.ax.yf[ar]);
       }
       if (staged) {
         if (yi >= 0) {

@@ -135,6 +135,19 @@ int rs_multislice_voxel(rs_plan* plan, void* u, void* U, const void* grid, int g
                         const double* slice_dz, const double* coord_scale,
                         int slice_begin, int slice_end, void* stream);
 
+/* rs_multislice_voxel over `batch` fields stacked in u and U (field k at u + k*nx*ny) that share
+ * the plan's size, the wavelength, the sample and its placement, and differ only in their
+ * content (e.g. the point sources of one energy in a multisim batch): each launch processes
+ * all of them, so small fields fill the GPU. The column passes run the per-block kernel
+ * batched over the fields; each field's result equals a separate rs_multislice_voxel call on it
+ * bit for bit unless the plan's schedule splits its columns. No reference counterpart
+ * (big-wave runs one source per process). */
+int rs_multislice_voxel_stacked(rs_plan* plan, int batch, void* u, void* U, const void* grid, int grid_signed,
+                                const float* db, int n_db, const rs_voxel_geom* geom,
+                                double dx, double dy, double wl, double cutoff,
+                                const double* slice_dz, const double* coord_scale,
+                                int slice_begin, int slice_end, void* stream);
+
 /* Plasma model scalars per energy (big-wave/plasma_sample.py:68-83, plasma.py:241-266).
  * planck_hc [eV*Angstrom] and r_electron_cm [cm] are the CODATA values the caller's
  * nist_lookup uses (nist_lookup/nist_lookup/physical_constants.py: PLANCK_HC, R_ELECTRON_CM). */

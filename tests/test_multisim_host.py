@@ -68,3 +68,14 @@ def test_reduce_detector_two_cpu_ranks():
     assert all(p.exitcode == 0 for p in procs)
     res = dict(q.get(timeout=5) for _ in range(2))
     assert res == {0: 64 * 3.0, 1: 64 * 3.0}
+
+
+def test_group_items_by_size_and_energy():
+    import importlib
+    ms = importlib.import_module("3d_ravesim_gb300.multisim")
+    It = ms.Item
+    items = [It(0.0, 0.0, 20e3, 256), It(1.0, 0.0, 20e3, 384), It(2.0, 0.0, 20e3, 256), It(3.0, 0.0, 25e3, 256),
+             It(4.0, 0.0, 20e3, 256), It(5.0, 0.0, 20e3, 256)]
+    groups = ms.group_items(items, 3)
+    assert [[it.x for it in g] for g in groups] == [[0.0, 2.0, 4.0], [5.0], [1.0], [3.0]]
+    assert sum(len(g) for g in groups) == len(items)
