@@ -381,8 +381,8 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
     """Batched multisim (64 jittered sources x 16 Kramers energies, grid sizes from {1024, 1536,
     2048, 3072}^2, 64-slice shell, 2048^2 area_v1 detector summed incoherently): the first `items`
     items through the fused multi-stream runner (eager and as one CUDA graph) and through the
-    loops of the plain unfused form (own FFTs, cuFFT); then the full 1024-item batch per item,
-    stacked by grid size and energy, and through the plain loop."""
+    loops of the plain unfused form (own FFTs, cuFFT); then the full 1024-item batch through the
+    fused runner and the plain loop."""
     ms = importlib.import_module("3d_ravesim_gb300.multisim")
     b = ms.shell_batch(max_items=items)
     fused = ms.BatchRunner(b, device, streams=2)  # 2 streams measured faster than 4 or 8 (0.96 vs 1.03 vs 1.05 s)
@@ -414,18 +414,14 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
     graphed.replay()
     out["fused_graph_s"] = round(time.perf_counter() - t0, 3)
     del graphed
-    # the full batch (1024 items, ~16 per grid size and energy): per item, and with the items of
-    # one size and energy stacked into one set of launches, against the plain loop
+    # the full batch (1024 items) through the fused runner and the plain loop
     full = ms.shell_batch()
-    stacked = ms.BatchRunner(full, device, streams=2)
-    stacked.run(full.items[:32], stacked=True)
     per_item = ms.BatchRunner(full, device, streams=2)
     per_item.run(full.items[:4])
     plain_full = ms.BatchRunner(full, device, streams=1)
     plain_full.run(full.items[:1], plain=True)
     full_out = {}
-    for name, runner, kw in (("fused_stacked", stacked, {"stacked": True}), ("fused_per_item", per_item, {}),
-                             ("plain_loop", plain_full, {"plain": True})):
+    for name, runner, kw in (("fused", per_item, {}), ("plain_loop", plain_full, {"plain": True})):
         runner.zero()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -433,7 +429,7 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
         torch.cuda.synchronize()
         full_out[name + "_s"] = round(time.perf_counter() - t0, 3)
     n_full = len(full.items)
-    del stacked, per_item, plain_full
+    del per_item, plain_full
     torch.cuda.empty_cache()
     slices = b.sample.grid.shape[0]
     res = {"case": f"{items} of 1024 items, sizes {b.info['sizes']}, {slices} slices each",
@@ -445,10 +441,9 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
            "speedup_vs_cufft_loop": round(out["plain_loop_cufft_s"] / min(out["fused_s"], out["fused_graph_s"]), 2),
            "graph_capture_s": round(capture_s, 2), **out,
            "full_batch": {"items": n_full,
-                          "fused_stacked_items_per_s": round(n_full / full_out["fused_stacked_s"], 2),
-                          "fused_per_item_items_per_s": round(n_full / full_out["fused_per_item_s"], 2),
+                          "fused_items_per_s": round(n_full / full_out["fused_s"], 2),
                           "plain_loop_items_per_s": round(n_full / full_out["plain_loop_s"], 2),
-                          "speedup": round(full_out["plain_loop_s"] / full_out["fused_stacked_s"], 2),
+                          "speedup": round(full_out["plain_loop_s"] / full_out["fused_s"], 2),
                           **full_out}}
     return res
 
