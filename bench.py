@@ -301,6 +301,68 @@ def accuracy_check(rs, torch, device, n: int, slices: int = 4, workload: str = "
             "detector_rel_l2": orc.relative_l2(gpu_det, ref_det)}
 
 
+def accuracy_plasma(rs, torch, device, n: int = 512, slices: int = 256) -> dict:
+    """Config 3's forward (Gaussian CH plasma, 8 keV, 256 x 2 um slices, the same 1.02 mm field)
+    at 512^2 (2 um pixels) through PlasmaSample.apply and the final leg, against the FP64
+    oracle's PlasmaSample restatement (big-wave/plasma_sample.py:126-233)."""
+    from scipy import fft as spfft
+
+    from oracle import bigwave_oracle as orc
+    wlmod = importlib.import_module("3d_ravesim_gb300.workloads")
+    psmod = importlib.import_module("3d_ravesim_gb300.plasma_sample")
+    w = wlmod.gaussian_plasma(n=n, slices=slices, dx=2e-6)
+    s, p = w.elements[0], w.params
+    u, U = rs.GpuVector(torch.ones(n * n, dtype=torch.complex64, device=device)), rs.GpuVector.zeros(n * n, device)
+    s.apply(u, U, p, w.cutoff, 0, None)
+    z = s.z_start + s.get_thickness()
+    rs.propagate_2d(u, U, p.dx, p.dy, p.wl, p.z_detector - z, p.chunk_size, w.cutoff, n, n, skip_fft=True)
+    gpu_det = rs.square_and_downsample_2d(u, p, p.z_detector)
+    gpu_u = u.to_numpy().reshape(n, n)
+    energy = rs.convert_energy_wavelength(p.wl)
+    with spfft.set_workers(os.cpu_count() or 1):
+        ru, rU = orc.plasma_apply_2d(np.ones((n, n), np.complex128), s.ne_grid, s.ni_grid, s.te_grid, s.zstar_grid,
+                                     s.scattering_factors, energy, psmod.codata_constants(), p.dx, p.dx, p.wl,
+                                     w.cutoff, s.pixel_size_x, s.pixel_size_y, s.pixel_size_z)
+        ru, _ = orc.propagate_2d(ru, p.dx, p.dx, p.wl, p.z_detector - z, w.cutoff, U=rU, skip_fft=True)
+    ref_det = orc.detector_area_v1(ru, p.dx, p.dx, p.detector_pixel_size_x, p.detector_pixel_size_y,
+                                   gpu_det.shape[1], gpu_det.shape[0], p.z_detector)
+    return {"case": f"Gaussian plasma (config 3 geometry) {n}^2 with {slices} slices vs FP64 oracle",
+            "field_rel_l2": orc.relative_l2(gpu_u, ru),
+            "intensity_rel_l2": orc.relative_l2(np.abs(gpu_u) ** 2, np.abs(ru) ** 2),
+            "detector_rel_l2": orc.relative_l2(gpu_det, ref_det)}
+
+
+def accuracy_multisim_item(rs, torch, device) -> dict:
+    """One item of the config-2 batch (the first 1024^2 one: point source, 64-slice shell, 10 m to
+    the 2048^2 detector) through the batch runner, against the FP64 oracle chain."""
+    from scipy import fft as spfft
+
+    from oracle import bigwave_oracle as orc
+    ms = importlib.import_module("3d_ravesim_gb300.multisim")
+    b = ms.shell_batch()
+    item = next(it for it in b.items if it.n == 1024)
+    runner = ms.BatchRunner(b, device, streams=1)
+    img = runner.run([item]).cpu().numpy()
+    gpu_u = runner._buffers(0, item.n)[0].to_numpy().reshape(item.n, item.n)
+    p = ms.item_params(b, item)
+    cutoff = b.cutoff_fraction / p.dx
+    smp = b.sample
+    db = ms._scaled_db(b, item.energy)
+    with spfft.set_workers(os.cpu_count() or 1):
+        u, U = orc.point_source_2d(item.n, item.n, p.dx, p.dx, b.z_sample, item.x, item.y, p.wl, cutoff)
+        u, U = orc.sample_apply_2d(u, np.asarray(smp.grid), db, p.dx, p.dx, p.wl, cutoff, smp.pixel_size_x,
+                                   smp.pixel_size_y, smp.pixel_size_z)
+        z = smp.z_start + smp.get_thickness()
+        u, U = orc.propagate_2d(u, p.dx, p.dx, p.wl, p.z_detector - z, cutoff, U=U, skip_fft=True)
+    ref = orc.detector_area_v1(u, p.dx, p.dx, p.detector_pixel_size_x, p.detector_pixel_size_y,
+                               b.detector_pixels, b.detector_pixels, p.z_detector)
+    return {"case": f"multisim item (config 2) 1024^2, {smp.grid.shape[0]} slices, {item.energy:.0f} eV "
+                    "vs FP64 oracle",
+            "field_rel_l2": orc.relative_l2(gpu_u, u),
+            "intensity_rel_l2": orc.relative_l2(np.abs(gpu_u) ** 2, np.abs(u) ** 2),
+            "detector_rel_l2": orc.relative_l2(img, ref)}
+
+
 def adjoint_cost(rs, torch, device, n: int = 2048, slices: int = 256, checkpoint_every=None) -> dict:
     """Gradient cost of the differentiable plasma workload (2048^2, 8 keV, 256 x 2 um slices of a
     Gaussian plasma, n0 = 1e21 cm^-3, L = 150 um, T_e = 500 eV): one forward pass against one
@@ -671,7 +733,9 @@ def run_ours(args):
         # and the benchmark size itself truncated to 4 sample slices
         line["accuracy"] = [accuracy_check(rs, torch, device, 1024, slices=args.slices),
                             accuracy_check(rs, torch, device, min(n, 4096)),
-                            accuracy_check(rs, torch, device, 1024, slices=128, workload="shell")]
+                            accuracy_check(rs, torch, device, 1024, slices=128, workload="shell"),
+                            accuracy_multisim_item(rs, torch, device),
+                            accuracy_plasma(rs, torch, device)]
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
