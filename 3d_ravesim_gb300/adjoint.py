@@ -13,7 +13,8 @@ scattered to the voxels through the bilinear weights. Slice fields are checkpoin
 `checkpoint_every` slices (default ~sqrt(nz)) and recomputed segment by segment on the way back;
 checkpoint_every=0 instead keeps the field entering every slice (written by the forward row
 pass itself), so the backward needs no recomputation: nz fields of nx*ny*8 bytes, 8.6 GB for
-256 slices at 2048^2, which a GB300's HBM holds easily.
+256 slices at 2048^2, which a GB300's HBM holds easily; checkpoint_every="auto" keeps every
+field when they fit a memory budget and checkpoints otherwise.
 """
 from __future__ import annotations
 
@@ -44,11 +45,18 @@ class MultisliceModel:
     """Detector image I(delta, beta) of a field u0 through a delta/beta voxel volume."""
 
     def __init__(self, params: SimParams, geom: VolumeGeometry, cutoff: float, u0: torch.Tensor,
-                 checkpoint_every: int | None = None):
+                 checkpoint_every: int | str | None = None, memory_budget_bytes: int | None = None):
+        """checkpoint_every: None (about sqrt(nz) slices per segment), a segment length, 0 (keep
+        every slice's field), or "auto": keep every field when nz fields fit memory_budget_bytes
+        (default: a quarter of the device's free memory at forward time), else sqrt(nz)."""
         self.p, self.geom, self.cutoff = params, geom, float(cutoff)
         self.u0 = u0
         self.device = u0.device
+        if not (checkpoint_every is None or checkpoint_every == "auto" or
+                (isinstance(checkpoint_every, int) and checkpoint_every >= 0)):
+            raise ValueError(f"checkpoint_every must be None, 'auto' or an int >= 0, got {checkpoint_every!r}")
         self.checkpoint_every = checkpoint_every
+        self.memory_budget_bytes = memory_budget_bytes
         n = params.nx * params.ny
         self.u = GpuVector(torch.empty(n, dtype=torch.complex64, device=self.device))
         self.U = GpuVector(torch.empty(n, dtype=torch.complex64, device=self.device))
@@ -89,11 +97,18 @@ class MultisliceModel:
         self.checkpoints = {}
         self.fields = None
         start = self.u.vec.clone()
-        if self.checkpoint_every == 0 and self.fused and self._forward_store_all(db):
+        mode = self.checkpoint_every
+        if mode == "auto":
+            need = nz * self.p.nx * self.p.ny * 8
+            budget = self.memory_budget_bytes
+            if budget is None:
+                budget = torch.cuda.mem_get_info(self.device)[0] // 4
+            mode = 0 if need <= budget else None
+        if mode == 0 and self.fused and self._forward_store_all(db):
             self.every = nz
             self.checkpoints[0] = start  # lets the per-slice backward recompute if it is forced
         else:
-            every = self.checkpoint_every or max(1, int(round(math.sqrt(nz))))
+            every = mode or max(1, int(round(math.sqrt(nz))))
             self.every = every
             for s0 in range(0, nz, every):
                 self.checkpoints[s0] = self.u.vec.clone()

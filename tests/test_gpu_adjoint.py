@@ -206,3 +206,19 @@ def test_fused_backward_matches_per_slice_at_1024(rs, cuda):
     assert model.last_backward == "per-slice"
     for c in (0, 1):
         assert rel_l2(g_fused[..., c], g_ref[..., c]) < 1e-4, c
+
+
+def test_auto_checkpointing_keeps_fields_within_budget(rs, cuda):
+    """checkpoint_every="auto": every slice's field when they fit the budget, sqrt(nz) segments
+    when not; both give the same gradient."""
+    grads = {}
+    for budget, keeps in ((1 << 40, True), (1, False)):
+        adj, model, db, p, geom = setup_case(rs, cuda, n=128, nz=9, every="auto", pitch=2e-6)
+        model.memory_budget_bytes = budget
+        dbt = torch.from_numpy(db).to(cuda)
+        I = model.forward(dbt)
+        assert (model.fields is not None) == keeps
+        assert model.every == (9 if keeps else 3)
+        grads[keeps] = model.backward(dbt, torch.ones_like(I)).cpu().numpy()
+        assert model.last_backward == "fused"
+    assert rel_l2(grads[True], grads[False]) < 1e-6

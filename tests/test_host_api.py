@@ -62,3 +62,16 @@ def test_slice_schedule_matches_cone_beam_geometry(rs):
     dz2, cs2 = oe.slice_schedule(p2, 0.5, 1e-6, 4)
     assert cs2 is not None and cs2[0] > 1.0
     assert dz2[0] == pytest.approx(1e-6 / (p2.fresnel_transverse_scale(0.5) * p2.fresnel_transverse_scale(0.5 + 1e-6)))
+
+
+def test_multislice_model_rejects_bad_checkpoint_setting():
+    import importlib
+    import torch
+    adj = importlib.import_module("3d_ravesim_gb300.adjoint")
+    rs = importlib.import_module("3d_ravesim_gb300")
+    p = rs.SimParams(N=64 * 64, nx=64, ny=64, dx=1e-6, dy=1e-6, z_detector=1.0, detector_size=64e-6,
+                     detector_pixel_size_x=1e-6, detector_pixel_size_y=1e-6, wl=1e-10, chunk_size=64)
+    geom = adj.VolumeGeometry(z_start=0.1, pixel_size_x=1e-6, pixel_size_y=1e-6, pixel_size_z=1e-6)
+    for bad in (-1, "sqrt", 2.5):
+        with pytest.raises(ValueError):
+            adj.MultisliceModel(p, geom, 1e5, torch.ones(64 * 64, dtype=torch.complex64), checkpoint_every=bad)
