@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=4096, help="field size (default 4096)")
     ap.add_argument("--slices", type=int, default=512)
+    ap.add_argument("--sweep-only", action="store_true",
+                    help="run only the FFT + propagate sweep of a four-step plan and print its JSON")
+    ap.add_argument("--sweep-n", type=int, default=32768, help="field size of the sweep (four-step plan)")
     ap.add_argument("--schedule", default="auto",
                     help="pass schedule of the field's plan: 'auto' (tuned at start-up) or a mask (1 pipelined "
                          "rows, 2 pipelined columns, 4 general row kernel, 8 split columns)")
@@ -510,13 +513,13 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
     return res
 
 
-def sweep_32768(rs, torch, device, reps: int = 5) -> dict:
+def sweep_32768(rs, torch, device, reps: int = 5, n: int = 32768) -> dict:
     """One FFT + propagate sweep at 32768^2 complex64 (8 GiB per field, the large-field case's
     roofline check): rs_propagate on a four-step plan, 30 keV, 50 nm pixels, 0.5 um step, the
-    circular cutoff active. The field (8 GiB) is far larger than L2, so no flush is needed."""
-    n = 32768
+    circular cutoff active. The field (8 GiB) is far larger than L2, so no flush is needed.
+    A smaller n (4096..16384) runs the same passes on a four-step plan of that size."""
     lib = rs._lib
-    plan = lib.plan_for(n, n, device)
+    plan = lib.plan_for(n, n, device) if n > 16384 else lib.Plan(n, n, device, flags=lib.RS_PLAN_FOURSTEP)
     g = torch.Generator(device="cpu").manual_seed(0)
     u = torch.polar(torch.ones(n * n // 64), torch.rand(n * n // 64, generator=g) * 6.283).to(torch.complex64)
     u = u.to(device).repeat(64)
@@ -553,7 +556,7 @@ def sweep_32768(rs, torch, device, reps: int = 5) -> dict:
         v["slice_step_frac"] = round(v["slice_step_GB_s"] / peak, 3)
     del u, U
     torch.cuda.empty_cache()
-    return {"case": "32768^2 c64 four-step plan (length-128 and length-256 transforms per axis), "
+    return {"case": f"{n}^2 c64 four-step plan (length-{n // 256} and length-256 transforms per axis), "
                     "30 keV, 50 nm pixels, dz 0.5 um, cutoff 0.45/dx",
             "peak_GB_s": peak, "peak_kind": kind,
             "slice_step_bytes": "32 B per pixel (2 field round trips, the single-pass minimum)",
@@ -573,6 +576,10 @@ def run_ours(args):
     device = torch.device("cuda", local)
     rs = importlib.import_module("3d_ravesim_gb300")
     rs.build()
+    if args.sweep_only:
+        if rank == 0:
+            print(json.dumps({"sweep": sweep_32768(rs, torch, device, n=args.sweep_n)}))
+        return
     wlmod = importlib.import_module("3d_ravesim_gb300.workloads")
     if args.workload == "capsule":
         w = wlmod.capsule_large(n=args.n, slices=args.slices)
