@@ -152,8 +152,8 @@ int check_plan(const rs_plan* p) {
 int check_plan_std(const rs_plan* p, const char* name) {
   RS_TRY(check_plan(p));
   if (p->four)
-    return fail(RS_EUNSUPPORTED, "%s: a four-step plan (%dx%d) supports rs_propagate, rs_point_source and "
-                "rs_detector only", name, p->nx, p->ny);
+    return fail(RS_EUNSUPPORTED, "%s: a four-step plan (%dx%d) supports rs_propagate, rs_point_source, "
+                "rs_point_source_propagate and rs_detector only", name, p->nx, p->ny);
   return RS_OK;
 }
 
@@ -934,10 +934,18 @@ static int source_propagate(rs_plan* p, void* u_, void* U_, const PointSrcArgs& 
 
 int rs_point_source_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double xs,
                               double ys, double z, double wl, double cutoff, void* stream) {
-  RS_TRY(check_plan_std(p, "rs_point_source_propagate"));
+  RS_TRY(check_plan(p));
   if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
   PointSrcArgs a{};
   RS_TRY(point_args(p, dx, dy, xs, ys, z, wl, a));
+  if (p->four) {
+    // the source field, then FFT -> cutoff -> IFFT as a four-step propagation of dz = 0 (its
+    // transfer tables are exactly 1); U is left in four-step storage order
+    cudaStream_t s = as_stream(stream);
+    RS_CK(launch_point_source(static_cast<float2*>(u_), p->nx, p->ny, a, s));
+    RS_TRY(build_prop(p, dx, dy, wl, 0.0, cutoff, true, s));
+    return propagate_four(p, static_cast<float2*>(u_), static_cast<float2*>(U_), false, s);
+  }
   return source_propagate(p, u_, U_, a, dx, dy, wl, cutoff, stream);
 }
 

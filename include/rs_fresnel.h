@@ -58,7 +58,8 @@ const char* rs_last_error(void);
  * with the W_n twiddle fused, then a length-256 transform, and the spectrum is kept in
  * four-step storage order (entry i of an axis holds frequency i/256 + (n/256)*(i%256)).
  * A four-step plan serves rs_propagate (U is left in that order; skip_fft expects it),
- * rs_point_source and rs_detector; the other entry points return RS_EUNSUPPORTED.
+ * rs_point_source, rs_point_source_propagate and rs_detector; the other entry points return
+ * RS_EUNSUPPORTED.
  * flags: 0, or RS_PLAN_FOURSTEP to ask for a four-step plan at 4096..16384 as well. */
 #define RS_PLAN_FOURSTEP 1u
 int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out);

@@ -187,3 +187,41 @@ def test_split_columns_16384(rs, cuda):
     finally:
         plan.set_schedule(old)
     assert rel_l2(out[8], out[0]) < 5e-6
+
+
+def test_point_source_propagate_four_step(rs, cuda):
+    """rs_point_source_propagate on a four-step plan (source field, then FFT -> cutoff -> IFFT as a
+    four-step propagation of dz = 0) against the single-pass plan."""
+    lib = rs._lib
+    n = 4096
+    four = lib.Plan(n, n, cuda, flags=lib.RS_PLAN_FOURSTEP)
+    std = lib.Plan(n, n, cuda)
+    dx, wl = 0.1e-6, rs.convert_energy_wavelength(25000.0)
+    out = []
+    for plan in (four, std):
+        u = torch.zeros(n * n, dtype=torch.complex64, device=cuda)
+        U = torch.zeros_like(u)
+        lib.check(lib.lib().rs_point_source_propagate(plan.handle, lib.ptr(u), lib.ptr(U), dx, dx, 2e-6, -1e-6, 1.0,
+                                                     wl, 0.4 / dx, lib.stream_handle()), "point source")
+        torch.cuda.synchronize()
+        out.append(u.cpu().numpy())
+    assert rel_l2(out[0], out[1]) < 4e-6
+
+
+def test_vacuum_run_32768(rs, cuda):
+    """run_simulation with no element at 32768^2 (point source 3 m before the detector): the
+    detected energy is the detector's solid angle, area / z^2, as in big-wave's vacuum runs."""
+    import importlib
+    ws = importlib.import_module("3d_ravesim_gb300.wavesim")
+    n, dx, z = 32768, 50e-9, 3.0
+    wl = rs.convert_energy_wavelength(30000.0)
+    p = rs.SimParams(N=n * n, nx=n, ny=n, dx=dx, dy=dx, z_detector=z, detector_size=4e-4, detector_size_x=4e-4,
+                     detector_size_y=4e-4, detector_pixel_size_x=8e-7, detector_pixel_size_y=8e-7, wl=wl,
+                     chunk_size=n)
+    u, U = rs.GpuVector.zeros(n * n, cuda), rs.GpuVector.zeros(n * n, cuda)
+    angle = float(np.arcsin(0.3 / dx * wl))
+    img = ws.run_simulation(p, rs.PointSource(x=0.0, y=0.0, z=0.0), [], [angle], u, U, [])[0]
+    assert img.shape == (500, 500)
+    assert abs(float(img.sum()) / ((4e-4) ** 2 / z ** 2) - 1) < 1e-4
+    del u, U
+    torch.cuda.empty_cache()
