@@ -88,10 +88,22 @@ __device__ __forceinline__ float2 cmulc_tw(float2 a, float4 w) {
 }
 #endif
 // x * (hi + lo) for a real constant split the same way, per lane of a pair
-__device__ __forceinline__ float mulk(float x, float hi, float lo) { return fmaf(hi, x, lo * x); }
+// (RS_COMP_CONST=0 drops the residual of the small DFTs' constants: an A/B switch)
+#ifndef RS_COMP_CONST
+#define RS_COMP_CONST 1
+#endif
+__device__ __forceinline__ float mulk(float x, float hi, float lo) {
+#if RS_COMP_CONST
+  return fmaf(hi, x, lo * x);
+#else
+  return hi * x;
+#endif
+}
 __device__ __forceinline__ float2 mulk2(float2 x, float hi, float lo) {
-#if RS_PACKED
+#if RS_PACKED && RS_COMP_CONST
   return __ffma2_rn(make_float2(hi, hi), x, __fmul2_rn(make_float2(lo, lo), x));
+#elif RS_PACKED
+  return __fmul2_rn(make_float2(hi, hi), x);
 #else
   return make_float2(mulk(x.x, hi, lo), mulk(x.y, hi, lo));
 #endif
@@ -134,7 +146,13 @@ __device__ __forceinline__ float2 tw16(float2 a) {
     constexpr float wil0 = (M == 1) ? -kS8lo : (M == 3) ? -kC8lo : kS8lo;
     constexpr float wi = INV ? -wi0 : wi0;
     constexpr float wil = INV ? -wil0 : wil0;
+#if RS_COMP_CONST
     return cmul_tw(a, make_float4(wr, wi, wrl, wil));
+#else
+    (void)wrl;
+    (void)wil;
+    return cmul(a, make_float2(wr, wi));
+#endif
   }
 }
 
