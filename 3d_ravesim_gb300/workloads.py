@@ -145,7 +145,7 @@ def talbot_lau(n: int = 4096, slices: int = 512, seed: int = 0, dx: float = 0.1e
 def gaussian_plasma(n: int = 2048, slices: int = 256, dx: float = 0.5e-6, energy: float = 8000.0,
                     n0: float = 1e21, length: float = 150e-6, te: float = 500.0, zstar: float = 3.5,
                     pz: float = 2e-6, pitch: float = 2e-6, z_detector_gap: float = 0.2):
-    """Config-3 forward: a plasma with n_e = n0 exp(-r^2 / 2 L^2) (cm^-3, r from the centre of the
+    """Differentiable-plasma forward (2048^2, 8 keV, 256 x 2 um slices): a plasma with n_e = n0 exp(-r^2 / 2 L^2) (cm^-3, r from the centre of the
     slab), T_e = 500 eV, Z* = 3.5 and n_i = n_e / Z*, in CH (zbar = 3.5, z2bar = 18.5), so q = 1 and
     only the free-electron refraction and the Kramers absorption contribute."""
     from .plasma_sample import PlasmaSample
@@ -175,7 +175,7 @@ def gaussian_plasma(n: int = 2048, slices: int = 256, dx: float = 0.5e-6, energy
 def capsule_large(n: int = 16384, slices: int = 1024, dx: float = 50e-9, energy: float = 30000.0,
                   seed: int = 0, pitch: float = 2e-6, pz: float = 0.5e-6, lmax: int = 8,
                   amplitude: float = 10e-6, z_source: float = 1.0, z_detector_gap: float = 0.3) -> Workload:
-    """Config-4 field: 16384^2 complex64 (2 GiB) at 30 keV, point source 1 m upstream, an
+    """Large in-HBM field: 16384^2 complex64 (2 GiB) at 30 keV, point source 1 m upstream, an
     ellipsoidal CH capsule shell (semi-axes 400/400/380 um, 15 um wall, delta 2.5e-7, beta
     1.5e-10) whose outer radius carries a seeded perturbation of real spherical harmonics
     l = 1..lmax scaled to `amplitude` at its largest, voxelised at `pitch` in x/y with one voxel

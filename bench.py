@@ -263,7 +263,7 @@ def cpu_baseline(n: int, samples: int = 2) -> dict:
 def accuracy_check(rs, torch, device, n: int, slices: int = 4, workload: str = "talbot") -> dict:
     """Relative L2 of field and detector intensity vs the FP64 oracle on the benchmark geometry at
     n^2 with `slices` sample slices (a full 512-slice FP64 run at 4096^2 takes hours on the CPU,
-    at 1024^2 about half a minute); workload "shell" is config 0 (plane wave, 1024^2, 128 slices)."""
+    at 1024^2 about half a minute); workload "shell" is the plane-wave shell case (1024^2, 128 slices)."""
     from scipy import fft as spfft
 
     from oracle import bigwave_oracle as orc
@@ -305,7 +305,7 @@ def accuracy_check(rs, torch, device, n: int, slices: int = 4, workload: str = "
 
 
 def accuracy_plasma(rs, torch, device, n: int = 512, slices: int = 256) -> dict:
-    """Config 3's forward (Gaussian CH plasma, 8 keV, 256 x 2 um slices, the same 1.02 mm field)
+    """The differentiable-plasma forward (Gaussian CH plasma, 8 keV, 256 x 2 um slices, the same 1.02 mm field)
     at 512^2 (2 um pixels) through PlasmaSample.apply and the final leg, against the FP64
     oracle's PlasmaSample restatement (big-wave/plasma_sample.py:126-233)."""
     from scipy import fft as spfft
@@ -329,14 +329,14 @@ def accuracy_plasma(rs, torch, device, n: int = 512, slices: int = 256) -> dict:
         ru, _ = orc.propagate_2d(ru, p.dx, p.dx, p.wl, p.z_detector - z, w.cutoff, U=rU, skip_fft=True)
     ref_det = orc.detector_area_v1(ru, p.dx, p.dx, p.detector_pixel_size_x, p.detector_pixel_size_y,
                                    gpu_det.shape[1], gpu_det.shape[0], p.z_detector)
-    return {"case": f"Gaussian plasma (config 3 geometry) {n}^2 with {slices} slices vs FP64 oracle",
+    return {"case": f"Gaussian plasma (2048^2-case geometry) {n}^2 with {slices} slices vs FP64 oracle",
             "field_rel_l2": orc.relative_l2(gpu_u, ru),
             "intensity_rel_l2": orc.relative_l2(np.abs(gpu_u) ** 2, np.abs(ru) ** 2),
             "detector_rel_l2": orc.relative_l2(gpu_det, ref_det)}
 
 
 def accuracy_multisim_item(rs, torch, device) -> dict:
-    """One item of the config-2 batch (the first 1024^2 one: point source, 64-slice shell, 10 m to
+    """One item of the multisim batch (the first 1024^2 one: point source, 64-slice shell, 10 m to
     the 2048^2 detector) through the batch runner, against the FP64 oracle chain."""
     from scipy import fft as spfft
 
@@ -359,7 +359,7 @@ def accuracy_multisim_item(rs, torch, device) -> dict:
         u, U = orc.propagate_2d(u, p.dx, p.dx, p.wl, p.z_detector - z, cutoff, U=U, skip_fft=True)
     ref = orc.detector_area_v1(u, p.dx, p.dx, p.detector_pixel_size_x, p.detector_pixel_size_y,
                                b.detector_pixels, b.detector_pixels, p.z_detector)
-    return {"case": f"multisim item (config 2) 1024^2, {smp.grid.shape[0]} slices, {item.energy:.0f} eV "
+    return {"case": f"multisim item 1024^2, {smp.grid.shape[0]} slices, {item.energy:.0f} eV "
                     "vs FP64 oracle",
             "field_rel_l2": orc.relative_l2(gpu_u, u),
             "intensity_rel_l2": orc.relative_l2(np.abs(gpu_u) ** 2, np.abs(u) ** 2),
@@ -418,7 +418,7 @@ def adjoint_cost(rs, torch, device, n: int = 2048, slices: int = 256, checkpoint
 
 
 def plasma_forward_rate(rs, torch, device, n: int = 2048, slices: int = 256, steps: int = 3) -> dict:
-    """Config-3 forward through PlasmaSample.apply: 2048^2, 8 keV, 256 x 2 um slices of a Gaussian
+    """The differentiable-plasma forward through PlasmaSample.apply: 2048^2, 8 keV, 256 x 2 um slices of a Gaussian
     plasma (n_e, n_i, T_e, Z* grids of 516^2 float32 per slice, delta/beta evaluated in the row pass)."""
     wlmod = importlib.import_module("3d_ravesim_gb300.workloads")
     w = wlmod.gaussian_plasma(n=n, slices=slices)
