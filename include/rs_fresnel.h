@@ -36,7 +36,7 @@ typedef enum rs_status {
   RS_EINVAL = 1,      /* bad argument / shape (Python maps to ValueError)        */
   RS_ENOMEM = 2,      /* device allocation failed                                  */
   RS_ECUDA = 3,       /* a CUDA runtime call failed                                */
-  RS_EUNSUPPORTED = 4,/* size/dtype outside what this build implements             */
+  RS_EUNSUPPORTED = 4,/* size/dtype outside what this library implements             */
   RS_ETIMEOUT = 5,    /* a bounded device wait gave up                             */
   RS_ECANCELLED = 6   /* host cancel flag observed between slices                  */
 } rs_status;
