@@ -108,6 +108,8 @@ struct rs_plan {
   float* yf = nullptr;
   void* det = nullptr;
   size_t det_cap = 0;
+  float2* plane = nullptr;  // one slice plane of plasma (delta, beta) for the voxel row kernel
+  size_t plane_cap = 0;
   // Geometry whose forward detector tables sit in `det` (valid = false after any other use of the
   // buffer). A repeated geometry needs neither the host build nor the copy; the copy matters,
   // because a pageable host->device copy first waits for all earlier work on its stream.
@@ -474,11 +476,30 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       pl.nyv = g->ny_v;
       pl.a = a;
     }
+    // Plasma slices on the voxel-only row kernel: the plane's (delta, beta) first, then the row
+    // pass reads them as a per-voxel volume (the same values and blends as the plasma row pass).
+    const bool plasma_plane = src.plasma && p->fast && p->row_vox && !src.store;
+    if (plasma_plane) {
+      if (p->plane_cap < plane) {
+        if (p->plane) RS_CK(cudaFree(p->plane));
+        p->plane = nullptr;
+        p->plane_cap = 0;
+        cudaError_t e = cudaMalloc(&p->plane, plane * sizeof(float2));
+        if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc for a plasma slice plane: %s", cudaGetErrorString(e));
+        p->plane_cap = plane;
+      }
+      RS_CK(launch_plasma_plane(pl, p->plane, static_cast<int>(plane), s));
+      vox = VoxelArgs{};
+      vox.dbv = p->plane;
+      vox.nxv = g->nx_v;
+      vox.nyv = g->ny_v;
+      vox.a = a;
+    }
     if (p->fast) {
       RowArgs r{};
       r.in = u; r.out = u; r.ny = p->ny * src.batch; r.tw = p->tws_x; r.ax = axis_tab(p);
       r.axis_rows = src.batch > 1 ? p->ny : 0;
-      r.flags = (z == s0 ? 0 : ROW_INV) | ROW_FWD | (src.plasma ? ROW_TPLASMA : ROW_TVOX);
+      r.flags = (z == s0 ? 0 : ROW_INV) | ROW_FWD | (src.plasma && !plasma_plane ? ROW_TPLASMA : ROW_TVOX);
       if (src.store) {
         r.flags |= ROW_STORE_U;
         r.aux = src.store + static_cast<size_t>(z - s0) * p->nx * p->ny;
@@ -747,6 +768,7 @@ int rs_plan_destroy(rs_plan* p) {
   for (cudaEvent_t e : p->ev_pool) cudaEventDestroy(e);
   cudaError_t e1 = cudaFree(p->arena);
   cudaError_t e2 = p->det ? cudaFree(p->det) : cudaSuccess;
+  if (p->plane && cudaFree(p->plane) != cudaSuccess) e2 = cudaErrorUnknown;
   if (dev != p->dev) cudaSetDevice(dev);
   delete p;
   if (e1 != cudaSuccess || e2 != cudaSuccess) return fail(RS_ECUDA, "cudaFree failed during plan destroy");

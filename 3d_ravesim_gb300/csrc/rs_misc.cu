@@ -274,6 +274,18 @@ cudaError_t launch_detector_adjoint(const DetAdjArgs& a, cudaStream_t s) {
   return counted(cudaGetLastError());
 }
 
+// delta, beta of every voxel of one plasma slice plane, for the voxel-only row kernel: the same
+// plasma_db_voxel values the plasma row pass computes, once per voxel instead of once per row.
+__global__ void plasma_plane_kernel(const PlasmaArgs pl, float2* dbv, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) dbv[i] = plasma_db_voxel(pl, i);
+}
+
+cudaError_t launch_plasma_plane(const PlasmaArgs& pl, float2* dbv, int count, cudaStream_t s) {
+  plasma_plane_kernel<<<nblocks(count), kTPB, 0, s>>>(pl, dbv, count);
+  return counted(cudaGetLastError());
+}
+
 cudaError_t launch_twiddles(float2* tw, int n, cudaStream_t s) {
   twiddle_kernel<<<nblocks(n), kTPB, 0, s>>>(tw, n);
   return counted(cudaGetLastError());

@@ -57,6 +57,8 @@ cudaError_t launch_scale(float2* u, size_t n, float scale, cudaStream_t s);
 cudaError_t launch_point_source(float2* u, int nx, int ny, const PointSrcArgs& p, cudaStream_t s);
 cudaError_t launch_transmission(float2* u, int nx, int ny, const AxisTab& ax, const VoxelArgs* vox,
                                 const PlasmaArgs* pl, cudaStream_t s);
+// (delta, beta) of the `count` voxels of one plasma slice plane into dbv.
+cudaError_t launch_plasma_plane(const PlasmaArgs& pl, float2* dbv, int count, cudaStream_t s);
 cudaError_t launch_detector(const DetArgs& a, cudaStream_t s);
 
 // Adjoint of one slice of the multislice forward u' = P (t * u): given v = P^H g' (in `v`),

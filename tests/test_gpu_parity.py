@@ -344,3 +344,26 @@ def test_fresnel_plane_fast_vs_oracle(rs, cuda, oracle, n):
     rs.PointSource(x=15e-6, y=7e-6, z=0.0).propagate_to(1.2, p, f := 0.4 / dx, u, U, None)
     ru, rU = oracle.fresnel_plane_2d(n, n, dx, dx, 1.2, 15e-6, 7e-6, wl, f)
     assert rel_l2(host(u, n, n), ru) < 1e-5
+
+
+def test_plasma_plane_path_is_bit_identical(rs, cuda):
+    """PlasmaSample.apply on the voxel-only row kernel (the slice plane's delta/beta evaluated
+    first) and on the general row kernel (delta/beta evaluated while staging each row) give
+    the same field bit for bit."""
+    wlmod = __import__("importlib").import_module("3d_ravesim_gb300.workloads")
+    w = wlmod.gaussian_plasma(n=512, slices=12, dx=2e-6)
+    s, p = w.elements[0], w.params
+    plan = rs._lib.plan_for(512, 512, cuda)
+    old = plan.schedule()
+    out = []
+    try:
+        for mask in (0, 4):  # 4: the general row kernel
+            plan.set_schedule(mask)
+            u = rs.GpuVector(torch.ones(512 * 512, dtype=torch.complex64, device=cuda))
+            U = rs.GpuVector.zeros(512 * 512, cuda)
+            s.apply(u, U, p, w.cutoff, 0, None)
+            torch.cuda.synchronize()
+            out.append((u.vec.clone(), U.vec.clone()))
+    finally:
+        plan.set_schedule(old)
+    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
