@@ -170,7 +170,7 @@ class MultisliceModel:
         p = self.p
         nz = db.shape[0]
         plan = _lib.plan_for(p.nx, p.ny, self.device)
-        if not plan.fast or p.nx & (p.nx - 1) or 3 * db.shape[2] > p.nx + p.nx // 16:
+        if not plan.fast or p.nx & (p.nx - 1) or 2 * db.shape[2] > p.nx + p.nx // 16:
             return False
         self.fields = torch.empty((nz, p.nx * p.ny), dtype=torch.complex64, device=self.device)
         with torch.cuda.device(self.device):

@@ -1125,8 +1125,8 @@ int rs_adjoint_multislice_dbgrid(rs_plan* p, void* g, const float* db_grid, cons
     return fail(RS_EINVAL, "slice range [%d, %d) outside [0, %d]", slice_begin, slice_end, geom->nz);
   if (!finite_pos(wl)) return fail(RS_EINVAL, "wavelength must be positive");
   const bool pow2 = (p->nx & (p->nx - 1)) == 0;
-  if (!p->fast || !pow2 || 3 * geom->nx_v > p->nx + p->nx / 16)
-    return fail(RS_EUNSUPPORTED, "fused adjoint needs power-of-two rows with nx_v <= (nx + nx/16)/3");
+  if (!p->fast || !pow2 || 2 * geom->nx_v > p->nx + p->nx / 16)
+    return fail(RS_EUNSUPPORTED, "fused adjoint needs power-of-two rows with nx_v <= (nx + nx/16)/2");
   if (slice_begin == slice_end) return RS_OK;
   cudaStream_t s = as_stream(stream);
   float2* gv = static_cast<float2*>(g);

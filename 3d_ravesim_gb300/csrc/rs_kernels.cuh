@@ -545,15 +545,17 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = valid ? a.in[rbase + slot_pos<N, RF>(t, e)] : make_float2(0.f, 0.f);
   }
-  float* acc = reinterpret_cast<float*>(buf + nxv);  // [2 rows][nxv][delta, beta]
+  // x-weighted gradient sums of the row, [nxv][delta, beta]; the y weights (1 - fy, fy) are the
+  // same for every pixel of the row, so they are applied once per voxel when the sums are added
+  // to the two voxel rows
+  float* acc = reinterpret_cast<float*>(buf + nxv);
   if (yi >= 0) {
     for (int j = t; j < nxv; j += T) buf[j] = voxel_col_blend(a.vox, j, yi, fy);
-    for (int j = t; j < 4 * nxv; j += T) acc[j] = 0.0f;
+    for (int j = t; j < 2 * nxv; j += T) acc[j] = 0.0f;
   }
   __syncthreads();
   if (yi >= 0) {
     const float k = 12.566370614359172f * a.vox.a;  // 4 pi t / wl
-    const float gy0 = 1.0f - fy;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int x = slot_pos<N, RF>(t, e);
@@ -569,24 +571,23 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
       const float gd = k * q.y, gb = -k * q.x;
       const float gx0 = 1.0f - fx;
       float* r0 = acc + 2 * xi;
-      float* r1 = acc + 2 * (nxv + xi);
-      atomicAdd(r0, gx0 * gy0 * gd);
-      atomicAdd(r0 + 1, gx0 * gy0 * gb);
-      atomicAdd(r0 + 2, fx * gy0 * gd);
-      atomicAdd(r0 + 3, fx * gy0 * gb);
-      atomicAdd(r1, gx0 * fy * gd);
-      atomicAdd(r1 + 1, gx0 * fy * gb);
-      atomicAdd(r1 + 2, fx * fy * gd);
-      atomicAdd(r1 + 3, fx * fy * gb);
+      atomicAdd(r0, gx0 * gd);
+      atomicAdd(r0 + 1, gx0 * gb);
+      atomicAdd(r0 + 2, fx * gd);
+      atomicAdd(r0 + 3, fx * gb);
       v[e] = cmulc(v[e], tr);               // conj(t) v
     }
   }
   __syncthreads();
   if (yi >= 0) {
     float* g0 = a.grad + static_cast<size_t>(yi) * nxv * 2;  // rows yi and yi + 1 are contiguous
-    for (int j = t; j < 4 * nxv; j += T) {
+    const float gy0 = 1.0f - fy;
+    for (int j = t; j < 2 * nxv; j += T) {
       const float val = acc[j];
-      if (val != 0.0f) atomicAdd(&g0[j], val);
+      if (val != 0.0f) {
+        atomicAdd(&g0[j], gy0 * val);
+        if (fy != 0.0f) atomicAdd(&g0[2 * nxv + j], fy * val);
+      }
     }
   }
   __syncthreads();  // the forward transform reuses the buffer

@@ -191,7 +191,7 @@ int rs_multislice_dbgrid_store(rs_plan* plan, void* u, void* U, const float* db_
  * per slice. On entry g = dL/dconj(u_end), the gradient with respect to the field leaving
  * slice_end - 1; on exit g = dL/dconj(u_begin). fields holds the fields entering each slice as
  * written by rs_multislice_dbgrid_store; dL/d(delta, beta) of every slice's voxels is added to
- * grad_grid (same layout as db_grid). Needs power-of-two rows and nx_v <= (nx + nx/16)/3
+ * grad_grid (same layout as db_grid). Needs power-of-two rows and nx_v <= (nx + nx/16)/2
  * (RS_EUNSUPPORTED otherwise; rs_adjoint_slice covers the rest). No counterpart in the reference
  * (big-wave has no gradients). */
 int rs_adjoint_multislice_dbgrid(rs_plan* plan, void* g, const float* db_grid, const rs_voxel_geom* geom, double dx,
