@@ -360,7 +360,10 @@ template <int N, int ROWS>
 #define RS_ROW_MINB_POW3 3
 #endif
 constexpr int row_minb() {
-  return ROWS * FftPlan<N>::T <= 256 ? (FftPlan<N>::E == 16 ? RS_ROW_MINB : RS_ROW_MINB_POW3) : 1;
+  // sized for 256-thread blocks; smaller blocks of short rows get proportionally more of them
+  return ROWS * FftPlan<N>::T <= 256
+             ? (FftPlan<N>::E == 16 ? RS_ROW_MINB : RS_ROW_MINB_POW3) * (256 / (ROWS * FftPlan<N>::T))
+             : 1;
 }
 
 // Shared memory of a row block: the exchange buffers (S per row), then a voxel-row prefetch

@@ -105,7 +105,14 @@ constexpr int box_rows(int n, int b = 256) { return (b <= 1 || n % b == 0) ? b :
 template <int N>
 struct ColPipeGeom {
   static constexpr int T = FftPlan<N>::T;
-  static constexpr int W = T >= 256 ? 2 : 512 / T;            // columns per strip (>= 2: 16-byte boxes)
+#ifndef RS_COLPIPE_THREADS
+#define RS_COLPIPE_THREADS 512
+#endif
+  // threads per strip: 256 at 1536 and 2048 (column passes 12 % and 10 % faster, measured),
+  // RS_COLPIPE_THREADS (512) elsewhere (256 was 7 % slower at 1024 and 3072)
+  static constexpr int THR = (N == 1536 || N == 2048) ? 256 : RS_COLPIPE_THREADS;
+  // columns per strip (>= 2: 16-byte boxes) for about THR threads
+  static constexpr int W = T >= THR / 2 ? 2 : THR / T;
   static constexpr int BH = box_rows(N);                      // rows per tensor-copy box
   static_assert(N % BH == 0, "the boxes must tile a column exactly");
   static constexpr int TILE = W * N;
