@@ -192,10 +192,12 @@ class Plan:
 
     @staticmethod
     def _destroy(handle: c_void_p, device: torch.device) -> None:
+        # a finaliser: it may run at interpreter exit, after torch's CUDA state or this module's
+        # globals are gone, where there is nothing left to free and nobody to report to
         try:
             with torch.cuda.device(device):
                 lib().rs_plan_destroy(handle)
-        except Exception:
+        except Exception:  # noqa: BLE001
             pass
 
 

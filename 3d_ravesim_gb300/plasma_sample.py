@@ -114,7 +114,9 @@ class PlasmaSample:
         return self.pixel_size_z * self._shape()[0]
 
     def store_deltabetas(self, deltabeta_table) -> None:
-        pass
+        """No table to store: the plasma's delta and beta come from its density, temperature and
+        charge grids (big-wave's PlasmaSample.store_deltabetas, plasma_sample.py:108-110, stores
+        nothing either)."""
 
     def _device_grids(self, device: torch.device):
         grids = (self.ne_grid, self.ni_grid, self.te_grid, self.zstar_grid)
