@@ -34,6 +34,8 @@ def plasma_delta_beta_grid_multi(ne, ni, te, zstar, f1bar, f2eff_bar, zbar, z2ba
     """Host FP64 restatement of big-wave/plasma.py:380-434 (used for checks and small tables)."""
     planck_hc, r_e = codata_constants()
     ne, ni, te, zstar = (np.asarray(a, dtype=np.float64) for a in (ne, ni, te, zstar))
+    if not (ne.shape == ni.shape == te.shape == zstar.shape):
+        raise ValueError("plasma grid tiles must have identical shapes")
     if energy <= 0.0:
         raise ValueError(f"energy must be positive, got {energy}")
     lamb_cm = 1.0e-8 * planck_hc / energy
