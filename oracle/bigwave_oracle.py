@@ -143,7 +143,8 @@ def interpolate_slice(values: np.ndarray, nx, ny, dx, dy, px, py, x_pos, y_pos, 
 
 def sample_transmission(grid_slice: np.ndarray, db_list: np.ndarray, nx, ny, dx, dy, px, py, pz, wl,
                         x_pos=0.0, y_pos=0.0, scale=1.0) -> np.ndarray:
-    """material_factor of the interpolated delta+i*beta of one Sample slice, complex128."""
+    """material_factor of the interpolated delta+i*beta of one Sample slice, complex128
+    (big-wave/optical_element.py:566-582: the db_list gather, the interpolation, the factor)."""
     db = interpolate_slice(db_list[grid_slice], nx, ny, dx, dy, px, py, x_pos, y_pos, scale)
     return material_factor(db, pz, wl)
 
@@ -215,6 +216,8 @@ def plasma_apply_2d(u, ne, ni, te, zs, sf, energy, consts, dx, dy, wl, cutoff, p
 
 # ---- detector (big-wave/propagation.py:949-1110) -----------------------------------------
 def _axis_plan(det, ds, n, sp):
+    """Fractional cell range [lo, hi) that each detector pixel covers on one grid axis, clipped to
+    the grid (big-wave/propagation.py:949-977, _area_axis_plan)."""
     gl = (-(n // 2) - 0.5) * sp
     gr = gl + n * sp
     lo = det - ds * 0.5
