@@ -539,6 +539,7 @@ struct DetTables {
   std::vector<int> xptr, xcell, yptr, ycell;
 };
 
+// Per-axis fractional overlap plan of the area_v1 detector (big-wave/propagation.py:949-977).
 void area_axis(int out_n, double ds, int grid_n, double sp, std::vector<double>& det,
                std::vector<double>& lo, std::vector<double>& hi, std::vector<long>& ilo,
                std::vector<double>& flo, std::vector<long>& ihi, std::vector<double>& fhi) {
@@ -563,6 +564,7 @@ void area_axis(int out_n, double ds, int grid_n, double sp, std::vector<double>&
   }
 }
 
+// area_v1 row and column weights: separable physical overlap areas (big-wave/propagation.py:995-1110).
 void build_area_v1(int nx, int ny, const rs_detector_geom& g, DetTables& t) {
   std::vector<double> xlo, xhi, ylo, yhi, fx0, fx1, fy0, fy1;
   std::vector<long> ix0, ix1, iy0, iy1;
@@ -603,6 +605,7 @@ void build_area_v1(int nx, int ny, const rs_detector_geom& g, DetTables& t) {
   }
 }
 
+// legacy_fastwave truncated ranges and count map (big-wave/propagation.py:836-946).
 void build_legacy(int nx, int ny, const rs_detector_geom& g, DetTables& t) {
   auto ranges = [](int out_n, int grid_n, double ds, double sp, std::vector<double>& det,
                    std::vector<long>& lo, std::vector<long>& hi) {
@@ -865,6 +868,7 @@ int rs_plan_profile_read(rs_plan* p, double* row_ms, double* col_ms, int* n_row,
   return RS_OK;
 }
 
+// NumpyVector.fft2 / ifft2 (big-wave/vector.py:341-347).
 int rs_fft2(rs_plan* p, const void* in, void* out, void* stream) {
   RS_TRY(check_plan_std(p, "rs_fft2"));
   if (!in || !out) return fail(RS_EINVAL, "NULL field pointer");
@@ -877,6 +881,7 @@ int rs_ifft2(rs_plan* p, const void* in, void* out, void* stream) {
   return ifft2_impl(p, static_cast<const float2*>(in), static_cast<float2*>(out), as_stream(stream));
 }
 
+// apply_frequency_cutoff_2d (big-wave/propagation.py:298-326).
 int rs_apply_cutoff(rs_plan* p, void* U, double freq, double dx, double dy, void* stream) {
   RS_TRY(check_plan_std(p, "rs_apply_cutoff"));
   if (!U) return fail(RS_EINVAL, "NULL field pointer");
@@ -896,6 +901,7 @@ int rs_apply_transfer(rs_plan* p, void* U, double dx, double dy, double wl, doub
   return RS_OK;
 }
 
+// propagate_2d (big-wave/propagation.py:396-442).
 int rs_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double wl, double dz,
                  double cutoff, int skip_fft, void* stream) {
   RS_TRY(check_plan(p));
@@ -941,6 +947,7 @@ static int point_args(rs_plan* p, double dx, double dy, double xs, double ys, do
   return RS_OK;
 }
 
+// propagate_analytically_2d (big-wave/propagation.py:458-484).
 int rs_point_source(rs_plan* p, void* u, double dx, double dy, double xs, double ys, double z,
                     double wl, void* stream) {
   RS_TRY(check_plan(p));
@@ -954,6 +961,7 @@ int rs_point_source(rs_plan* p, void* u, double dx, double dy, double xs, double
 static int source_propagate(rs_plan* p, void* u_, void* U_, const PointSrcArgs& a, double dx, double dy,
                             double wl, double cutoff, void* stream);
 
+// PointSource.propagate_to without Fresnel scaling (big-wave/source.py:97-107).
 int rs_point_source_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double xs,
                               double ys, double z, double wl, double cutoff, void* stream) {
   RS_TRY(check_plan(p));
@@ -971,6 +979,7 @@ int rs_point_source_propagate(rs_plan* p, void* u_, void* U_, double dx, double 
   return source_propagate(p, u_, U_, a, dx, dy, wl, cutoff, stream);
 }
 
+// Fresnel-scaled source plane (big-wave/source.py:62-95).
 int rs_fresnel_plane(rs_plan* p, void* u, double dx, double dy, double xs, double ys, double dz, double wl,
                      void* stream) {
   RS_TRY(check_plan(p));
@@ -1023,6 +1032,7 @@ static int source_propagate(rs_plan* p, void* u_, void* U_, const PointSrcArgs& 
   return RS_OK;
 }
 
+// Sample._apply_2d (big-wave/optical_element.py:502-596).
 int rs_multislice_voxel(rs_plan* p, void* u, void* U, const void* grid, int grid_signed, const float* db,
                         int n_db, const rs_voxel_geom* geom, double dx, double dy, double wl,
                         double cutoff, const double* slice_dz, const double* coord_scale,
@@ -1056,6 +1066,7 @@ int rs_multislice_voxel_stacked(rs_plan* p, int batch, void* u, void* U, const v
                     slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
 }
 
+// PlasmaSample._apply_2d (big-wave/plasma_sample.py:126-233).
 int rs_multislice_plasma(rs_plan* p, void* u, void* U, const void* ne, const void* ni, const void* te,
                          const void* zstar, int grid_f64, const rs_plasma_consts* pc,
                          const rs_voxel_geom* geom, double dx, double dy, double wl, double cutoff,
@@ -1309,6 +1320,7 @@ int rs_apply_transmission_voxel(rs_plan* p, void* u, const void* grid, int grid_
   return RS_OK;
 }
 
+// square_and_downsample_2d (big-wave/propagation.py:1113-1130).
 int rs_detector(rs_plan* p, const void* u, double* out, const rs_detector_geom* g, void* stream) {
   RS_TRY(check_plan(p));
   if (!u || !out || !g) return fail(RS_EINVAL, "NULL pointer argument");

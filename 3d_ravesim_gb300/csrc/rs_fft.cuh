@@ -1,4 +1,6 @@
 // rs_fft.cuh — register-resident Stockham FFT for lengths 2^k and 3*2^k (16..16384).
+// The transforms behind NumpyVector.fft2 / ifft2 (big-wave/vector.py:341-347: scipy.fft, forward
+// unnormalised, inverse scaled by 1/N), fused with the per-slice operators by the passes.
 //
 // Each sequence of length N is processed by T = N/E threads that each hold E complex values
 // in registers (E = 16, or 24 for 3*2^k). A stage of radix R performs E/R butterflies per
