@@ -1,6 +1,5 @@
 """Shared fixtures. `-m gpu` tests need a CUDA device and the native library; the rest run on CPU."""
 import importlib
-import os
 import sys
 from pathlib import Path
 

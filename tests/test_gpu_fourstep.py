@@ -2,7 +2,6 @@
 transforms against the single-pass plan and the FP64 oracle at 4096/8192, the spectrum in
 four-step storage order, skip_fft chaining, and at 32768^2 the dz / -dz round trip and
 Parseval (no FP64 reference fits the host there)."""
-import ctypes
 
 import numpy as np
 import pytest
