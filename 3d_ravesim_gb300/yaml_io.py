@@ -39,10 +39,38 @@ def _scalar(v: Any) -> str:
             return ".inf" if f > 0 else "-.inf"
         return repr(f)
     s = str(v)
+    if any(not _printable(c) for c in s):
+        return _double_quoted(s)
     if (s in _RESERVED or s in _SPECIAL or _INT.match(s) or _FLOAT.match(s) or s != s.strip()
-            or any(c in s for c in ":#{}[],&*!|>'\"%@`\n\t") or s.startswith(("-", "?"))):
+            or any(c in s for c in ":#{}[],&*!|>'\"%@`") or s.startswith(("-", "?"))):
         return "'" + s.replace("'", "''") + "'"
     return s
+
+
+def _printable(c: str) -> bool:
+    """YAML's printable set (YAML 1.2, section 5.1) minus the line breaks."""
+    o = ord(c)
+    return (0x20 <= o <= 0x7E or 0xA0 <= o <= 0xD7FF or 0xE000 <= o <= 0xFFFD
+            or 0x10000 <= o <= 0x10FFFF) and o not in (0x2028, 0x2029, 0xFEFF)
+
+
+_ESC_OUT = {"\\": "\\\\", '"': '\\"', "\n": "\\n", "\t": "\\t", "\r": "\\r", "\0": "\\0"}
+
+
+def _double_quoted(s: str) -> str:
+    out = []
+    for c in s:
+        if c in _ESC_OUT:
+            out.append(_ESC_OUT[c])
+        elif _printable(c):
+            out.append(c)
+        elif ord(c) <= 0xFF:
+            out.append(f"\\x{ord(c):02x}")
+        elif ord(c) <= 0xFFFF:
+            out.append(f"\\u{ord(c):04x}")
+        else:
+            out.append(f"\\U{ord(c):08x}")
+    return '"' + "".join(out) + '"'
 
 
 def _emit(v: Any, indent: int, out: list[str]) -> None:
@@ -105,9 +133,9 @@ def _parse_scalar(s: str) -> Any:
             raise ValueError(f"unterminated quoted scalar {s!r}")
         return s[1:-1].replace("''", "'")
     if s.startswith('"'):
-        if not s.endswith('"') or len(s) < 2:
+        if not s.endswith('"') or len(s) < 2 or _quote_end(s, 0) != len(s) - 1:
             raise ValueError(f"unterminated quoted scalar {s!r}")
-        return bytes(s[1:-1], "utf-8").decode("unicode_escape")
+        return _unescape(s[1:-1])
     s = _strip_tag(s)
     if s in ("", "~", "null", "Null", "NULL"):
         return None
@@ -130,16 +158,71 @@ def _parse_scalar(s: str) -> Any:
     return s
 
 
+_ESC_IN = {"0": "\0", "a": "\a", "b": "\b", "t": "\t", "\t": "\t", "n": "\n", "v": "\v", "f": "\f",
+           "r": "\r", "e": "\x1b", " ": " ", '"': '"', "/": "/", "\\": "\\", "N": "\x85", "_": "\xa0",
+           "L": "\u2028", "P": "\u2029"}
+
+
+def _unescape(body: str) -> str:
+    """The escapes of a double-quoted YAML scalar (YAML 1.2, section 5.7)."""
+    out = []
+    i = 0
+    while i < len(body):
+        c = body[i]
+        if c != "\\":
+            out.append(c)
+            i += 1
+            continue
+        if i + 1 >= len(body):
+            raise ValueError(f"dangling escape in {body!r}")
+        e = body[i + 1]
+        width = {"x": 2, "u": 4, "U": 8}.get(e)
+        if width:
+            digits = body[i + 2:i + 2 + width]
+            if len(digits) != width or any(d not in "0123456789abcdefABCDEF" for d in digits):
+                raise ValueError(f"bad escape in {body!r}")
+            out.append(chr(int(digits, 16)))
+            i += 2 + width
+        elif e in _ESC_IN:
+            out.append(_ESC_IN[e])
+            i += 2
+        else:
+            raise ValueError(f"unknown escape \\{e} in {body!r}")
+    return "".join(out)
+
+
+def _quote_end(text: str, start: int) -> int:
+    """Index of the quote closing the quoted scalar opening at text[start], or -1: a single-quoted
+    scalar escapes its quote by doubling it, a double-quoted one by a backslash."""
+    q = text[start]
+    j = start + 1
+    while j < len(text):
+        c = text[j]
+        if q == '"' and c == "\\":
+            j += 2
+            continue
+        if c == q:
+            if q == "'" and j + 1 < len(text) and text[j + 1] == "'":
+                j += 2
+                continue
+            return j
+        j += 1
+    return -1
+
+
 def _strip_comment(line: str) -> str:
-    quote = None
-    for i, c in enumerate(line):
-        if quote:
-            if c == quote:
-                quote = None
-        elif c in "'\"":
-            quote = c
-        elif c == "#" and (i == 0 or line[i - 1] in " \t"):
+    i = 0
+    while i < len(line):
+        c = line[i]
+        if c in "'\"" and (i == 0 or line[i - 1] in " \t:-[{,"):
+            end = _quote_end(line, i)
+            if end < 0:
+                return line.rstrip()
+            i = end + 1
+            continue
+        if c == "#" and (i == 0 or line[i - 1] in " \t"):
             return line[:i].rstrip()
+        i += 1
     return line.rstrip()
 
 
@@ -154,15 +237,9 @@ def _strip_tag(text: str) -> str:
 def _split_key(text: str):
     """'key: value' -> (key, value) honouring a quoted key; None if text is not a mapping entry."""
     if text.startswith(("'", '"')):
-        q = text[0]
-        j = 1
-        while j < len(text):
-            if text[j] == q:
-                if q == "'" and j + 1 < len(text) and text[j + 1] == "'":
-                    j += 2
-                    continue
-                break
-            j += 1
+        j = _quote_end(text, 0)
+        if j < 0:
+            return None
         rest = text[j + 1:]
         if rest.startswith(":") and (len(rest) == 1 or rest[1] == " "):
             return _parse_scalar(text[:j + 1]), rest[1:].strip()
@@ -175,7 +252,8 @@ def _split_key(text: str):
 
 def loads(text: str) -> Any:
     lines = []
-    for raw in text.splitlines():
+    # only \n (and \r\n) break lines: str.splitlines would also split at control characters
+    for raw in text.replace("\r\n", "\n").split("\n"):
         if raw.strip() in ("---", "...") or not raw.strip() or raw.lstrip().startswith("#"):
             continue
         line = _strip_comment(raw)
