@@ -89,3 +89,27 @@ def test_cancel_token_interrupts_save(ck, tmp_path):
         ck.RunCheckpoint(tmp_path, FINGERPRINT, cancel_token=Token()).save(
             Field(64), Field(64), current_z=0.0, element_index=0, slice_index=0, u_fourier_valid=False, stage="s")
     assert not (tmp_path / "manifest.json").exists()
+
+
+def test_interrupted_save_keeps_the_previous_generation_and_no_parts(ck, tmp_path):
+    a = ck.RunCheckpoint(tmp_path, FINGERPRINT)
+    u0, U0 = Field(64), Field(64)
+    u0.vec = torch.randn(64, dtype=torch.complex64, generator=torch.Generator().manual_seed(4))
+    a.save(u0, U0, current_z=0.5, element_index=1, slice_index=2, u_fourier_valid=True, stage="sample")
+    before = sorted(p.name for p in tmp_path.iterdir())
+
+    class Token:
+        calls = 0
+
+        def is_cancelled(self):  # lets the u vector be written, cancels before U
+            Token.calls += 1
+            return Token.calls > 1
+    with pytest.raises(InterruptedError):
+        ck.RunCheckpoint(tmp_path, FINGERPRINT, cancel_token=Token()).save(
+            Field(64), Field(64), current_z=0.75, element_index=1, slice_index=3, u_fourier_valid=True, stage="s")
+    assert sorted(p.name for p in tmp_path.iterdir()) == before
+    u1, U1 = Field(64), Field(64)
+    st = a.load(u1, U1)
+    assert (st.current_z, st.slice_index) == (0.5, 2)
+    assert np.array_equal(np.asarray(u1.vec), np.asarray(u0.vec))
+
