@@ -31,6 +31,18 @@ def test_z_steps_match_bigwave(hm, golden):
         off += n
 
 
+def test_z_steps_match_bigwave_broadly(hm):
+    """186 (dz, hist_dz) pairs from big-wave's own rule (tests/golden/make_history_zsteps_golden.py):
+    exact and inexact multiples, tails just above and below half a step, dz below one step."""
+    import json
+    from pathlib import Path
+    cases = json.loads((Path(__file__).parent / "golden" / "history_zsteps.json").read_text())
+    assert len(cases) > 150
+    for c in cases:
+        z = hm._history_z_steps(c["dz"], c["hist_dz"])
+        assert z.dtype == np.float64 and z.tolist() == c["z"], (c["dz"], c["hist_dz"])
+
+
 def test_memory_history_matches_bigwave(hm, golden):
     h = hm.History(roi=(1, 9, 2, 11), downsample=(2, 3))
     for i, f in enumerate(golden["mem_frames_in"]):
