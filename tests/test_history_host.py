@@ -105,12 +105,19 @@ def test_progress_and_1d_frames(hm):
     assert h.metadata()["format_version"] == 1 and h.metadata()["axis_order"] == ["x", "z"]
 
 
-def test_streaming_needs_h5py(hm, tmp_path, monkeypatch):
-    """A History that has to stream (storage path and budget 0) says so when h5py is absent."""
-    monkeypatch.setattr(hm, "_h5py", lambda: None)
+def test_streaming_is_refused(hm, tmp_path):
+    """A History big-wave would stream to HDF5 (storage path and budget 0, or a budget the frames
+    outgrow, or resuming a stream) says so before writing anything."""
     h = hm.History(storage_path=tmp_path / "history.h5", memory_budget_bytes=0)
     with pytest.raises(RuntimeError, match="h5py"):
         h.push(np.zeros((4, 4)), 0.1)
+    h = hm.History(storage_path=tmp_path / "history.h5", memory_budget_bytes=200)
+    h.push(np.zeros((4, 4)), 0.1)
+    with pytest.raises(RuntimeError, match="in memory"):
+        h.push(np.zeros((4, 4)), 0.2)
+    (tmp_path / "old.h5").write_bytes(b"")
+    with pytest.raises(RuntimeError):
+        hm.History(storage_path=tmp_path / "old.h5", resume=True)
     # under budget it stays in memory
     h = hm.History(storage_path=tmp_path / "history.h5", memory_budget_bytes=1 << 20)
     h.push(np.zeros((4, 4)), 0.1)
