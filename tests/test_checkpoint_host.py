@@ -113,3 +113,20 @@ def test_interrupted_save_keeps_the_previous_generation_and_no_parts(ck, tmp_pat
     assert (st.current_z, st.slice_index) == (0.5, 2)
     assert np.array_equal(np.asarray(u1.vec), np.asarray(u0.vec))
 
+
+
+def test_slice_checkpointer_saves_every_cadence_slice():
+    ws = importlib.import_module("3d_ravesim_gb300.wavesim")
+    saved = []
+
+    class Recorder:
+        def save(self, u, U, **state):
+            saved.append((u, U, state))
+    cb = ws._slice_checkpointer(Recorder(), "u", "U", 2)
+    n = ws.CHECKPOINT_SLICE_CADENCE
+    for k in range(1, 2 * n + 2):
+        cb(k, 0.5 + 1e-6 * k)
+    assert [s[2]["slice_index"] for s in saved] == [n, 2 * n]
+    assert saved[0][:2] == ("u", "U")
+    assert saved[0][2] == {"current_z": 0.5 + 1e-6 * n, "element_index": 2, "slice_index": n,
+                           "u_fourier_valid": True, "stage": "element_slice"}
