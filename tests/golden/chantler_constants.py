@@ -64,4 +64,6 @@ def main(root: Path):
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    from _refroot import reference_root
+    main(reference_root())

@@ -1,6 +1,6 @@
 """Generate tests/golden/bigwave_golden.npz by running big-wave itself on seeded inputs.
 
-Run in a checkout that has the RAVE-SIM sources (default /root/reference, or pass the path):
+Run in a checkout that has the RAVE-SIM sources (pass its path, or set $RAVESIM_REFERENCE):
     python tests/golden/make_golden.py [/path/to/RAVE-SIM]
 big-wave is imported with stub modules for its optional dependencies (bfpy, ruamel.yaml,
 h5py, nist_lookup.xraydb_plugin), none of which the 2D in-memory path uses; `import config`
@@ -217,4 +217,6 @@ def main(root: Path) -> None:
 
 
 if __name__ == "__main__":
-    main(Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference"))
+    sys.path.insert(0, str(Path(__file__).resolve().parent))
+    from _refroot import reference_root
+    main(reference_root())
