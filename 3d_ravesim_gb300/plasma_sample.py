@@ -13,7 +13,7 @@ from typing import Callable, Optional, Union
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, chantler
 from .optical_element import slice_schedule, upload_grid
 from .propagation import SimParams, convert_energy_wavelength, require_row_aligned_chunk_size
 from .vector import as_gpu_pair
@@ -67,7 +67,8 @@ class PlasmaSample:
 
     The per-energy Chantler scalars (f1bar, f2eff_bar, zbar, z2bar) come from
     `scattering_factors` (a tuple, or a callable energy -> tuple). When it is unset they are
-    looked up through nist_lookup exactly as the reference does, which needs its database.
+    computed from nist_lookup's Chantler database by this package's own lookup (`chantler`):
+    the compound average of `formula`, else the single element Z.
     """
 
     z_start: float
@@ -89,15 +90,14 @@ class PlasmaSample:
         if sf is not None:
             return tuple(float(v) for v in (sf(energy) if callable(sf) else sf))  # type: ignore[return-value]
         try:
-            import plasma as ref_plasma  # the reference module, when it is importable
-        except ImportError as exc:
+            chantler.database_path()
+        except FileNotFoundError as exc:
             raise RuntimeError(
                 "PlasmaSample needs scattering_factors=(f1bar, f2eff_bar, zbar, z2bar) when "
                 "nist_lookup's Chantler database is not available") from exc
         if self.formula:
-            return ref_plasma.compound_scattering_factors(self.formula, energy)
-        scat = ref_plasma._get_scatterer(ref_plasma._get_element_symbol(int(self.Z)), energy)
-        return scat.f1, scat.f2 * (scat.mu_total / scat.mu_photo), float(self.Z), float(self.Z) ** 2
+            return chantler.compound_scattering_factors(self.formula, energy)
+        return chantler.element_scattering_factors(int(self.Z), energy)
 
     def _shape(self) -> tuple:
         return tuple(self.ne_grid.shape)
