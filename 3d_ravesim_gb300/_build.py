@@ -20,7 +20,7 @@ INCLUDE = ROOT / "include"
 # -DRS_PACKED_F32X2=0 variant built side by side for comparison).
 BUILD = Path(os.environ.get("RS_BUILD_DIR", PKG / "_build"))
 LIB = BUILD / "librs_fresnel.so"
-SOURCES = ["rs_pass_pow2_rows.cu", "rs_pass_pow2_cols.cu", "rs_pass_pow3_rows.cu", "rs_pass_pow3_cols.cu",
+SOURCES = ["rs_pass_pow2_rows.cu", "rs_pass_pow2_cols.cu", "rs_pass_pow3_rows.cu", "rs_pass_pow3_cols.cu", "rs_pass_x2.cu",
            "rs_dispatch.cu", "rs_misc.cu", "rs_abi.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 

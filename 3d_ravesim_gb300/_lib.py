@@ -79,6 +79,12 @@ _SIGS = {
     "rs_plan_get_schedule": ([_P, ctypes.POINTER(c_int)], c_int),
     "rs_plan_schedules": ([_P, ctypes.POINTER(c_int), c_int, ctypes.POINTER(c_int)], c_int),
     "rs_plan_status": ([_P, ctypes.POINTER(c_int)], c_int),
+    "rs_plan_check": ([_P, ctypes.POINTER(c_int)], c_int),
+    "rs_plan_clear_status": ([_P, _P], c_int),
+    "rs_plan_test_stall": ([_P, c_int], c_int),
+    "rs_detector_table_bytes": ([c_int, c_int, ctypes.POINTER(DetectorGeom), ctypes.POINTER(ctypes.c_size_t)], c_int),
+    "rs_plan_reserve": ([_P, ctypes.c_size_t, ctypes.c_size_t], c_int),
+    "rs_alloc_count": ([ctypes.POINTER(ctypes.c_ulonglong)], c_int),
     "rs_detector_noalloc": ([_P, c_int, c_int, _P, ctypes.POINTER(DetectorGeom), _P], c_int),
     "rs_launch_count": ([ctypes.POINTER(ctypes.c_ulonglong)], c_int),
     "rs_plan_profile": ([_P, c_int], c_int),
@@ -178,10 +184,10 @@ class Plan:
 
     def schedules(self) -> list[int]:
         """The schedule masks that are distinct for this plan's sizes."""
-        buf = (c_int * 16)()
+        buf = (c_int * 64)()
         n = c_int(0)
-        check(lib().rs_plan_schedules(self.handle, buf, 16, ctypes.byref(n)), "rs_plan_schedules")
-        return [buf[i] for i in range(min(n.value, 16))]
+        check(lib().rs_plan_schedules(self.handle, buf, 64, ctypes.byref(n)), "rs_plan_schedules")
+        return [buf[i] for i in range(min(n.value, 64))]
 
     def status(self) -> int:
         """Synchronise and return the device status word (0 = no bounded wait gave up)."""
@@ -189,6 +195,31 @@ class Plan:
         with torch.cuda.device(self.device):
             check(lib().rs_plan_status(self.handle, ctypes.byref(st)), "rs_plan_status")
         return st.value
+
+    def check(self) -> None:
+        """Raise TimeoutError if a pipelined pass of this plan gave up waiting for a bulk copy.
+        No device synchronisation: the answer is as of the last call whose stream the caller has
+        synchronised. The status is cleared after it is reported once."""
+        st = c_int(0)
+        code = lib().rs_plan_check(self.handle, ctypes.byref(st))
+        if code != RS_OK:
+            msg = lib().rs_last_error().decode(errors="replace")
+            self.clear_status()
+            check(code, f"plan {self.nx}x{self.ny}: {msg}")
+
+    def clear_status(self) -> None:
+        with torch.cuda.device(self.device):
+            check(lib().rs_plan_clear_status(self.handle, stream_handle(self.device)), "rs_plan_clear_status")
+
+    def test_stall(self, enable: bool = True) -> None:
+        """Test hook: the next pipelined column pass times out on purpose (bounded, no fault)."""
+        check(lib().rs_plan_test_stall(self.handle, int(bool(enable))), "rs_plan_test_stall")
+
+    def reserve(self, detector_table_bytes: int = 0, plasma_plane_voxels: int = 0) -> None:
+        """Grow the plan's detector-table and plasma-plane buffers now, so a run allocates nothing."""
+        with torch.cuda.device(self.device):
+            check(lib().rs_plan_reserve(self.handle, int(detector_table_bytes), int(plasma_plane_voxels)),
+                  "rs_plan_reserve")
 
     @staticmethod
     def _destroy(handle: c_void_p, device: torch.device) -> None:
@@ -229,6 +260,29 @@ def plan_for(nx: int, ny: int, device: torch.device, slot: int | None = None) ->
         from . import autotune
         autotune.apply_to_plan(p)  # the cached pass schedule of this device and size, if any
     return p
+
+
+def check_plans(device: torch.device | None = None) -> None:
+    """After a host synchronisation: raise TimeoutError if any pass of this device's plans gave up
+    waiting for a bulk copy (see Plan.check)."""
+    idx = None if device is None else (device.index if device.index is not None else torch.cuda.current_device())
+    for (nx, ny, d, k), p in list(_plans.items()):
+        if idx is None or d == idx:
+            p.check()
+
+
+def detector_table_bytes(nx: int, ny: int, geom: DetectorGeom) -> int:
+    n = ctypes.c_size_t(0)
+    check(lib().rs_detector_table_bytes(int(nx), int(ny), ctypes.byref(geom), ctypes.byref(n)),
+          "rs_detector_table_bytes")
+    return int(n.value)
+
+
+def alloc_count() -> int:
+    """Device and pinned-host allocations made by the native library so far in this process."""
+    n = ctypes.c_ulonglong(0)
+    check(lib().rs_alloc_count(ctypes.byref(n)), "rs_alloc_count")
+    return int(n.value)
 
 
 def launch_count() -> int:

@@ -20,6 +20,7 @@
 #include "rs_fresnel.h"
 #include "rs_misc.cuh"
 #include "rs_pipe_api.cuh"
+#include "rs_x2_api.cuh"
 
 using namespace rs;
 
@@ -60,6 +61,12 @@ constexpr bool kDefaultPipeRows = RS_DEFAULT_PIPE_ROWS != 0;
 constexpr bool kDefaultPipeCols = true;
 
 std::atomic<unsigned long long> g_launches{0};
+std::atomic<unsigned long long> g_allocs{0};  // device and pinned allocations made by this library
+
+cudaError_t counted_malloc(void** ptr, size_t bytes) {
+  g_allocs.fetch_add(1, std::memory_order_relaxed);
+  return cudaMalloc(ptr, bytes);
+}
 
 bool finite_pos(double v) { return std::isfinite(v) && v > 0.0; }
 
@@ -125,8 +132,24 @@ struct rs_plan {
   bool pipe_cols = true;
   bool row_vox = true;
   int* status = nullptr;  // device word set by bounded waits that gave up
+  // Pinned copy of `status`, refreshed by a 4-byte copy queued at the end of every call that ran a
+  // pipelined pass (status_pending), so a host that has synchronised its stream can read it
+  // without another device synchronisation (rs_plan_check).
+  volatile int* status_host = nullptr;
+  bool status_pending = false;
+  int test_stall = 0;     // one-shot: the next pipelined column pass waits on a barrier nobody completes
+  // Split-pair multislice passes (rs_x2.cuh): kDitherTables dithered copies of the row stage table
+  // and of the two-level column table, and the matching DFT constants; slice k uses copy k mod K.
+  bool x2r_on = true, x2c_on = true;  // schedule: cleared by RS_SCHED_COMP_ROWS / RS_SCHED_COMP_COLS
+  bool x2_rows = false, x2_cols = false;  // available for this plan's sizes
+  void* twd_arena = nullptr;
+  float4* twd_x = nullptr;
+  float4* twd_y2 = nullptr;
+  int twd_x_len = 0, twd_y2_len = 0;
+  DftConsts kconst[kDitherTables];
   struct MapEntry {
     const void* ptr = nullptr;
+    int w = 0, bh = 0;
     CUtensorMap map;
   };
   MapEntry maps[4];
@@ -207,6 +230,20 @@ int build_axes(rs_plan* p, const rs_voxel_geom* g, double dx, double dy, double 
 
 AxisTab axis_tab(const rs_plan* p) { return AxisTab{p->xi, p->xf, p->yi, p->yf, p->xp}; }
 
+// At the end of an entry point that ran pipelined passes: queue the copy of the device status
+// word into the plan's pinned host word on the caller's stream (stream-ordered, no host sync).
+struct StatusNote {
+  rs_plan* p;
+  cudaStream_t s;
+  StatusNote(rs_plan* plan, void* stream) : p(plan), s(static_cast<cudaStream_t>(stream)) {}
+  ~StatusNote() {
+    if (p && p->status_pending && p->status_host) {
+      p->status_pending = false;
+      cudaMemcpyAsync(const_cast<int*>(p->status_host), p->status, sizeof(int), cudaMemcpyDeviceToHost, s);
+    }
+  }
+};
+
 // ---- pipelined passes -------------------------------------------------------------------
 PFN_cuTensorMapEncodeTiled_v12000 g_encode = nullptr;
 
@@ -228,7 +265,7 @@ bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 
 // Tensor map of a (ny, nx) complex64 field viewed as 8-byte elements, box (w columns, bh rows).
 const CUtensorMap* field_map(rs_plan* p, const void* base, int w, int bh) {
   for (auto& m : p->maps)
-    if (m.ptr == base) return &m.map;
+    if (m.ptr == base && m.w == w && m.bh == bh) return &m.map;
   auto& slot = p->maps[p->map_next];
   p->map_next = (p->map_next + 1) % 4;
   cuuint64_t dims[2] = {static_cast<cuuint64_t>(p->nx), static_cast<cuuint64_t>(p->ny)};
@@ -243,13 +280,17 @@ const CUtensorMap* field_map(rs_plan* p, const void* base, int w, int bh) {
     return nullptr;
   }
   slot.ptr = base;
+  slot.w = w;
+  slot.bh = bh;
   return &slot.map;
 }
 
 cudaError_t run_row(rs_plan* p, const RowArgs& r, cudaStream_t s) {
   if (p->pipe_rows && !(r.flags & ROW_STORE_U) && row_pipe_ok(p->nx) && (r.flags & ROW_SRC || aligned16(r.in)) &&
-      aligned16(r.out))
+      aligned16(r.out)) {
+    p->status_pending = true;
     return launch_row_pipe(p->nx, r, p->status, s);
+  }
   return launch_row_pass(p->nx, r, s, p->row_vox);
 }
 
@@ -290,10 +331,42 @@ cudaError_t run_col(rs_plan* p, const ColArgs& ca, cudaStream_t s) {
     if (mi) {
       const CUtensorMap in_copy = *mi;
       const CUtensorMap* mo = field_map(p, c.out, w, bh);
-      if (mo) return launch_col_pipe(p->ny, c, in_copy, *mo, p->status, s);
+      if (mo) {
+        p->status_pending = true;
+        c.test_stall = p->test_stall;
+        p->test_stall = 0;
+        return launch_col_pipe(p->ny, c, in_copy, *mo, p->status, s);
+      }
     }
   }
   return launch_col_pass(p->ny, c, s);
+}
+
+// The multislice column pass on split pairs with table j (rs_x2.cuh), when the plan's schedule
+// and sizes allow it; otherwise the column pass of the schedule. Returns cudaErrorNotSupported
+// through `used` = false so the caller can tell which ran.
+cudaError_t run_col_ms(rs_plan* p, const ColArgs& ca, int j, bool* used, cudaStream_t s) {
+  *used = false;
+  int w = 0, bh = 0;
+  if (p->x2c_on && p->x2_cols && ca.batches <= 1 && col_x2_box(p->ny, &w, &bh) && aligned16(ca.in) &&
+      aligned16(ca.out) && tensor_map_encoder()) {
+    const CUtensorMap* mi = field_map(p, ca.in, w, bh);
+    if (mi) {
+      const CUtensorMap in_copy = *mi;
+      const CUtensorMap* mo = field_map(p, ca.out, w, bh);
+      if (mo) {
+        ColArgs c = ca;
+        c.twd = p->twd_y2 + static_cast<size_t>(j) * p->twd_y2_len;
+        c.kc = p->kconst[j];
+        c.test_stall = p->test_stall;
+        p->test_stall = 0;
+        p->status_pending = true;
+        *used = true;
+        return launch_col_x2(p->ny, c, in_copy, *mo, p->status, s);
+      }
+    }
+  }
+  return run_col(p, ca, s);
 }
 
 // Records a start event before a pass when profiling is on; returns the pair index or -1.
@@ -316,6 +389,33 @@ int prof_begin(rs_plan* p, int kind, cudaStream_t s) {
 void prof_end(rs_plan* p, int idx, cudaStream_t s) {
   if (idx >= 0) cudaEventRecord(p->ev_pool[idx + 1], s);
 }
+
+// ---- buffers that grow with the geometry (sized up front by rs_plan_reserve) --------------
+// Growing one frees the old buffer (cudaFree waits for the work still using it) and allocates a
+// larger one; rs_plan_reserve does this before a run so that the run itself allocates nothing.
+int grow_det(rs_plan* p, size_t bytes) {
+  if (bytes <= p->det_cap) return RS_OK;
+  p->det_cache.valid = false;
+  if (p->det) RS_CK(cudaFree(p->det));
+  p->det = nullptr;
+  p->det_cap = 0;
+  cudaError_t e = counted_malloc(&p->det, bytes);
+  if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc(%zu) for detector tables: %s", bytes, cudaGetErrorString(e));
+  p->det_cap = bytes;
+  return RS_OK;
+}
+
+int grow_plane(rs_plan* p, size_t voxels) {
+  if (voxels <= p->plane_cap) return RS_OK;
+  if (p->plane) RS_CK(cudaFree(p->plane));
+  p->plane = nullptr;
+  p->plane_cap = 0;
+  cudaError_t e = counted_malloc(reinterpret_cast<void**>(&p->plane), voxels * sizeof(float2));
+  if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc for a plasma slice plane: %s", cudaGetErrorString(e));
+  p->plane_cap = voxels;
+  return RS_OK;
+}
+
 
 // ---- building blocks (stream-ordered, no host sync) ----------------------------------
 int fft2_impl(rs_plan* p, const float2* in, float2* out, cudaStream_t s) {
@@ -440,6 +540,13 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
   const float a = static_cast<float>(g->pixel_size_z / wl);
   const float inv_n = static_cast<float>(1.0 / (static_cast<double>(p->nx) * p->ny));
 
+  // Split-pair row passes (voxel transmission only: ids, per-voxel delta/beta or a plasma plane);
+  // slice z's forward transform and slice z + 1's inverse use dithered table z mod K, so every
+  // transform is undone by one with the same table.
+  const bool plasma_rows_vox = !src.plasma || (p->fast && p->row_vox && !src.store);
+  const bool x2r = p->fast && p->x2r_on && p->x2_rows && !src.store && plasma_rows_vox &&
+                   g->nx_v <= row_x2_slots(p->nx);
+  auto table_x = [&](int z) { return p->twd_x + static_cast<size_t>(z % kDitherTables) * p->twd_x_len; };
   double cur_dz = NAN, cur_cs = NAN;
   for (int z = s0; z < s1; ++z) {
     const double dz = slice_dz[z];
@@ -480,14 +587,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
     // pass reads them as a per-voxel volume (the same values and blends as the plasma row pass).
     const bool plasma_plane = src.plasma && p->fast && p->row_vox && !src.store;
     if (plasma_plane) {
-      if (p->plane_cap < plane) {
-        if (p->plane) RS_CK(cudaFree(p->plane));
-        p->plane = nullptr;
-        p->plane_cap = 0;
-        cudaError_t e = cudaMalloc(&p->plane, plane * sizeof(float2));
-        if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc for a plasma slice plane: %s", cudaGetErrorString(e));
-        p->plane_cap = plane;
-      }
+      RS_TRY(grow_plane(p, plane));
       RS_CK(launch_plasma_plane(pl, p->plane, static_cast<int>(plane), s));
       vox = VoxelArgs{};
       vox.dbv = p->plane;
@@ -507,7 +607,17 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       r.vox = vox;
       r.pl = pl;
       const int er = prof_begin(p, 0, s);
-      RS_CK(run_row(p, r, s));
+      if (x2r) {
+        r.twd_fwd = table_x(z);
+        r.k_fwd = p->kconst[z % kDitherTables];
+        if (z != s0) {
+          r.twd_inv = table_x(z - 1);
+          r.k_inv = p->kconst[(z - 1) % kDitherTables];
+        }
+        RS_CK(launch_row_x2(p->nx, r, s));
+      } else {
+        RS_CK(run_row(p, r, s));
+      }
       prof_end(p, er, s);
       ColArgs c{};
       c.in = u; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tws_y;
@@ -518,7 +628,8 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
         c.bstride = static_cast<long long>(p->nx) * p->ny;
       }
       const int ec = prof_begin(p, 1, s);
-      RS_CK(run_col(p, c, s));
+      bool col_x2 = false;
+      RS_CK(run_col_ms(p, c, z % kDitherTables, &col_x2, s));
       prof_end(p, ec, s);
     } else {
       RS_TRY(generic_slice(p, u, U, src.plasma ? nullptr : &vox, src.plasma ? &pl : nullptr, s));
@@ -527,7 +638,13 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
   if (p->fast) {
     RowArgs r{};
     r.in = u; r.out = u; r.ny = p->ny * src.batch; r.tw = p->tws_x; r.flags = ROW_INV;
-    RS_CK(run_row(p, r, s));
+    if (x2r) {
+      r.twd_inv = table_x(s1 - 1);
+      r.k_inv = p->kconst[(s1 - 1) % kDitherTables];
+      RS_CK(launch_row_x2(p->nx, r, s));
+    } else {
+      RS_CK(run_row(p, r, s));
+    }
   }
   return RS_OK;
 }
@@ -538,6 +655,7 @@ struct DetTables {
   std::vector<float> xw;
   std::vector<int> xptr, xcell, yptr, ycell;
 };
+
 
 // Per-axis fractional overlap plan of the area_v1 detector (big-wave/propagation.py:949-977).
 void area_axis(int out_n, double ds, int grid_n, double sp, std::vector<double>& det,
@@ -637,7 +755,38 @@ void build_legacy(int nx, int ny, const rs_detector_geom& g, DetTables& t) {
 
 size_t align8(size_t v) { return (v + 7) & ~static_cast<size_t>(7); }
 
+// Byte offsets of the forward detector tables in one buffer; returns the buffer size.
+size_t det_layout(const DetTables& t, size_t o[8]) {
+  o[0] = 0;                                     // xdet
+  o[1] = o[0] + align8(t.xdet.size() * 8);      // ydet
+  o[2] = o[1] + align8(t.ydet.size() * 8);      // yw
+  o[3] = o[2] + align8(t.yw.size() * 8);        // xw
+  o[4] = o[3] + align8(t.xw.size() * 4);        // xptr
+  o[5] = o[4] + align8(t.xptr.size() * 4);      // xcell
+  o[6] = o[5] + align8(t.xcell.size() * 4);     // yptr
+  o[7] = o[6] + align8(t.yptr.size() * 4);      // ycell
+  return o[7] + align8(t.ycell.size() * 4) + 8;
+}
+
 }  // namespace
+
+// Dithered copies of cos(pi/8), sin(pi/8) and sqrt(2)/2 for the split-pair DFTs: in copy j each
+// constant is one of the two floats bracketing its exact value, the upper one in a fraction of
+// the copies equal to the exact value's position between them (the rule of the twiddle tables).
+void dither_consts(DftConsts* k) {
+  const double exact[3] = {std::cos(M_PI / 8.0), std::sin(M_PI / 8.0), std::sqrt(0.5)};
+  float out[3][kDitherTables];
+  for (int c = 0; c < 3; ++c) {
+    const float h = static_cast<float>(exact[c]);
+    const double l = exact[c] - static_cast<double>(h);
+    const float other = std::nextafter(h, l > 0 ? INFINITY : -INFINITY);
+    const double frac = l == 0.0 ? 0.0 : l / (static_cast<double>(other) - static_cast<double>(h));
+    const int n_other = static_cast<int>(std::lround(frac * kDitherTables));
+    const int off = (17 * c + 5) % kDitherTables;
+    for (int j = 0; j < kDitherTables; ++j) out[c][j] = ((j + off) % kDitherTables) < n_other ? other : h;
+  }
+  for (int j = 0; j < kDitherTables; ++j) k[j] = DftConsts{out[0][j], out[1][j], out[2][j]};
+}
 
 // ======================================================================== extern "C"
 extern "C" {
@@ -694,8 +843,20 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   const size_t o_kyi = take(fy4 ? sizeof(int) * ny : 0);
   const size_t o_p4y = take(fy4 ? sizeof(float4) * ny : 0);
   const size_t o_eys = take(split ? sizeof(float2) * ny : 0);
-  e = cudaMalloc(&p->arena, bytes);
+  e = counted_malloc(&p->arena, bytes);
   if (e != cudaSuccess) { delete p; return fail(RS_ENOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e)); }
+  {
+    void* h = nullptr;
+    g_allocs.fetch_add(1, std::memory_order_relaxed);
+    e = cudaHostAlloc(&h, sizeof(int), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      cudaFree(p->arena);
+      delete p;
+      return fail(RS_ENOMEM, "cudaHostAlloc of the status word: %s", cudaGetErrorString(e));
+    }
+    p->status_host = static_cast<volatile int*>(h);
+    *p->status_host = 0;
+  }
   char* c = static_cast<char*>(p->arena);
   if (fast) {
     p->tws_x = reinterpret_cast<float4*>(c + o_twx);
@@ -756,8 +917,36 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   if (e == cudaSuccess) e = cudaStreamSynchronize(0);
   if (e != cudaSuccess) {
     cudaFree(p->arena);
+    cudaFreeHost(const_cast<int*>(p->status_host));
     delete p;
     return fail(RS_ECUDA, "twiddle setup: %s", cudaGetErrorString(e));
+  }
+  // split-pair multislice passes: dithered tables derived from the compensated ones
+  if (fast && (nx & (nx - 1)) == 0 && (ny & (ny - 1)) == 0) {
+    int w = 0, bh = 0;
+    p->x2_rows = row_x2_ok(nx);
+    p->x2_cols = col_x2_box(ny, &w, &bh) && p->tw2_y != nullptr;
+    p->twd_x_len = p->x2_rows ? static_cast<int>(twx) : 0;
+    p->twd_y2_len = p->x2_cols ? static_cast<int>(tw2y) : 0;
+    const size_t n = static_cast<size_t>(p->twd_x_len + p->twd_y2_len) * kDitherTables;
+    if (n > 0) {
+      e = counted_malloc(&p->twd_arena, n * sizeof(float4));
+      if (e == cudaSuccess) {
+        p->twd_x = static_cast<float4*>(p->twd_arena);
+        p->twd_y2 = p->twd_x + static_cast<size_t>(p->twd_x_len) * kDitherTables;
+        if (p->x2_rows) e = launch_dither_tables(p->tws_x, p->twd_x, p->twd_x_len, 0);
+        if (e == cudaSuccess && p->x2_cols) e = launch_dither_tables(p->tw2_y, p->twd_y2, p->twd_y2_len, 0);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(0);
+      }
+      if (e != cudaSuccess) {
+        if (p->twd_arena) cudaFree(p->twd_arena);
+        cudaFree(p->arena);
+        cudaFreeHost(const_cast<int*>(p->status_host));
+        delete p;
+        return fail(RS_ECUDA, "dithered table setup: %s", cudaGetErrorString(e));
+      }
+    }
+    dither_consts(p->kconst);
   }
   *out = p;
   return RS_OK;
@@ -772,6 +961,8 @@ int rs_plan_destroy(rs_plan* p) {
   cudaError_t e1 = cudaFree(p->arena);
   cudaError_t e2 = p->det ? cudaFree(p->det) : cudaSuccess;
   if (p->plane && cudaFree(p->plane) != cudaSuccess) e2 = cudaErrorUnknown;
+  if (p->status_host && cudaFreeHost(const_cast<int*>(p->status_host)) != cudaSuccess) e2 = cudaErrorUnknown;
+  if (p->twd_arena && cudaFree(p->twd_arena) != cudaSuccess) e2 = cudaErrorUnknown;
   if (dev != p->dev) cudaSetDevice(dev);
   delete p;
   if (e1 != cudaSuccess || e2 != cudaSuccess) return fail(RS_ECUDA, "cudaFree failed during plan destroy");
@@ -791,8 +982,11 @@ int rs_plan_set_pipeline(rs_plan* p, int mask) {
 
 int rs_plan_set_schedule(rs_plan* p, int mask) {
   RS_TRY(check_plan(p));
-  if (mask & ~(RS_SCHED_PIPE_ROWS | RS_SCHED_PIPE_COLS | RS_SCHED_ROW_GENERAL | RS_SCHED_SPLIT_COLS))
+  if (mask & ~(RS_SCHED_PIPE_ROWS | RS_SCHED_PIPE_COLS | RS_SCHED_ROW_GENERAL | RS_SCHED_SPLIT_COLS |
+               RS_SCHED_COMP_ROWS | RS_SCHED_COMP_COLS))
     return fail(RS_EINVAL, "unknown schedule bits 0x%x", mask);
+  p->x2r_on = (mask & RS_SCHED_COMP_ROWS) == 0;
+  p->x2c_on = (mask & RS_SCHED_COMP_COLS) == 0;
   p->pipe_rows = (mask & RS_SCHED_PIPE_ROWS) != 0;
   p->pipe_cols = (mask & RS_SCHED_PIPE_COLS) != 0;
   p->row_vox = (mask & RS_SCHED_ROW_GENERAL) == 0;
@@ -804,7 +998,8 @@ int rs_plan_get_schedule(const rs_plan* p, int* mask) {
   RS_TRY(check_plan(p));
   if (!mask) return fail(RS_EINVAL, "mask is NULL");
   *mask = (p->pipe_rows ? RS_SCHED_PIPE_ROWS : 0) | (p->pipe_cols ? RS_SCHED_PIPE_COLS : 0) |
-          (p->row_vox ? 0 : RS_SCHED_ROW_GENERAL) | (p->split_cols ? RS_SCHED_SPLIT_COLS : 0);
+          (p->row_vox ? 0 : RS_SCHED_ROW_GENERAL) | (p->split_cols ? RS_SCHED_SPLIT_COLS : 0) |
+          (p->x2r_on ? 0 : RS_SCHED_COMP_ROWS) | (p->x2c_on ? 0 : RS_SCHED_COMP_COLS);
   return RS_OK;
 }
 
@@ -817,7 +1012,13 @@ int rs_plan_schedules(const rs_plan* p, int* masks, int cap, int* count) {
   const bool rows_pipe = p->fast && row_pipe_ok(p->nx);
   const bool cols_pipe = p->fast && col_pipe_box(p->ny, &w, &bh);
   int n = 0;
-  for (int m = 0; m < 16; ++m) {
+  for (int m = 0; m < 64; ++m) {
+    // a direction without split-pair passes has only its single-sequence kernels; where the
+    // split-pair passes run, the bits that choose among that direction's other kernels change nothing
+    if ((m & RS_SCHED_COMP_ROWS) && !p->x2_rows) continue;
+    if ((m & RS_SCHED_COMP_COLS) && !p->x2_cols) continue;
+    if (!(m & RS_SCHED_COMP_ROWS) && p->x2_rows && (m & (RS_SCHED_PIPE_ROWS | RS_SCHED_ROW_GENERAL))) continue;
+    if (!(m & RS_SCHED_COMP_COLS) && p->x2_cols && (m & (RS_SCHED_PIPE_COLS | RS_SCHED_SPLIT_COLS))) continue;
     if ((m & RS_SCHED_SPLIT_COLS) && !p->split_ok) continue;
     if ((m & RS_SCHED_PIPE_ROWS) && !rows_pipe) continue;
     if ((m & RS_SCHED_PIPE_COLS) && !cols_pipe) continue;
@@ -834,7 +1035,61 @@ int rs_plan_status(rs_plan* p, int* device_status) {
   if (!device_status) return fail(RS_EINVAL, "device_status is NULL");
   RS_CK(cudaDeviceSynchronize());
   RS_CK(cudaMemcpy(device_status, p->status, sizeof(int), cudaMemcpyDeviceToHost));
+  *p->status_host = *device_status;
   if (*device_status != 0) return fail(RS_ETIMEOUT, "a pipelined pass gave up waiting for a bulk copy");
+  return RS_OK;
+}
+
+int rs_plan_check(const rs_plan* p, int* device_status) {
+  if (!p) return fail(RS_EINVAL, "plan is NULL");
+  const int st = *p->status_host;
+  if (device_status) *device_status = st;
+  if (st != 0)
+    return fail(RS_ETIMEOUT, "a pipelined pass of this plan gave up waiting for a bulk copy; the field it "
+                "wrote is not valid");
+  return RS_OK;
+}
+
+int rs_plan_clear_status(rs_plan* p, void* stream) {
+  RS_TRY(check_plan(p));
+  RS_CK(cudaMemsetAsync(p->status, 0, sizeof(int), as_stream(stream)));
+  RS_CK(cudaStreamSynchronize(as_stream(stream)));
+  *p->status_host = 0;
+  return RS_OK;
+}
+
+int rs_plan_test_stall(rs_plan* p, int enable) {
+  if (!p) return fail(RS_EINVAL, "plan is NULL");
+  p->test_stall = enable ? 1 : 0;
+  return RS_OK;
+}
+
+int rs_detector_table_bytes(int nx, int ny, const rs_detector_geom* g, size_t* bytes) {
+  if (!g || !bytes) return fail(RS_EINVAL, "NULL pointer argument");
+  if (nx <= 0 || ny <= 0) return fail(RS_EINVAL, "nx and ny must be positive");
+  if (g->out_x <= 0 || g->out_y <= 0) return fail(RS_EINVAL, "detector output must be non-empty");
+  if (!finite_pos(g->dx) || !finite_pos(g->dy) || !finite_pos(g->ds_px) || !finite_pos(g->ds_py))
+    return fail(RS_EINVAL, "detector and grid spacings must be positive");
+  if (!std::isfinite(g->detector_z) || g->detector_z == 0.0) return fail(RS_EINVAL, "detector z must be finite and non-zero");
+  DetTables t;
+  if (g->integrator == 0) build_area_v1(nx, ny, *g, t);
+  else if (g->integrator == 1) build_legacy(nx, ny, *g, t);
+  else return fail(RS_EINVAL, "unknown integrator %d", g->integrator);
+  size_t o[8];
+  *bytes = det_layout(t, o);
+  return RS_OK;
+}
+
+int rs_plan_reserve(rs_plan* p, size_t detector_table_bytes, size_t plasma_plane_voxels) {
+  RS_TRY(check_plan(p));
+  RS_TRY(grow_det(p, detector_table_bytes));
+  RS_TRY(grow_plane(p, plasma_plane_voxels));
+  return RS_OK;
+}
+
+int rs_alloc_count(unsigned long long* out) {
+  if (!out) return fail(RS_EINVAL, "out is NULL");
+  *out = g_allocs.load(std::memory_order_relaxed);
   return RS_OK;
 }
 
@@ -870,12 +1125,14 @@ int rs_plan_profile_read(rs_plan* p, double* row_ms, double* col_ms, int* n_row,
 
 // NumpyVector.fft2 / ifft2 (big-wave/vector.py:341-347).
 int rs_fft2(rs_plan* p, const void* in, void* out, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_fft2"));
   if (!in || !out) return fail(RS_EINVAL, "NULL field pointer");
   return fft2_impl(p, static_cast<const float2*>(in), static_cast<float2*>(out), as_stream(stream));
 }
 
 int rs_ifft2(rs_plan* p, const void* in, void* out, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_ifft2"));
   if (!in || !out) return fail(RS_EINVAL, "NULL field pointer");
   return ifft2_impl(p, static_cast<const float2*>(in), static_cast<float2*>(out), as_stream(stream));
@@ -883,6 +1140,7 @@ int rs_ifft2(rs_plan* p, const void* in, void* out, void* stream) {
 
 // apply_frequency_cutoff_2d (big-wave/propagation.py:298-326).
 int rs_apply_cutoff(rs_plan* p, void* U, double freq, double dx, double dy, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_apply_cutoff"));
   if (!U) return fail(RS_EINVAL, "NULL field pointer");
   cudaStream_t s = as_stream(stream);
@@ -893,6 +1151,7 @@ int rs_apply_cutoff(rs_plan* p, void* U, double freq, double dx, double dy, void
 
 int rs_apply_transfer(rs_plan* p, void* U, double dx, double dy, double wl, double dz, double cutoff,
                       void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_apply_transfer"));
   if (!U) return fail(RS_EINVAL, "NULL field pointer");
   cudaStream_t s = as_stream(stream);
@@ -904,6 +1163,7 @@ int rs_apply_transfer(rs_plan* p, void* U, double dx, double dy, double wl, doub
 // propagate_2d (big-wave/propagation.py:396-442).
 int rs_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double wl, double dz,
                  double cutoff, int skip_fft, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan(p));
   if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
   float2* u = static_cast<float2*>(u_);
@@ -950,6 +1210,7 @@ static int point_args(rs_plan* p, double dx, double dy, double xs, double ys, do
 // propagate_analytically_2d (big-wave/propagation.py:458-484).
 int rs_point_source(rs_plan* p, void* u, double dx, double dy, double xs, double ys, double z,
                     double wl, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan(p));
   if (!u) return fail(RS_EINVAL, "NULL field pointer");
   PointSrcArgs a{};
@@ -964,6 +1225,7 @@ static int source_propagate(rs_plan* p, void* u_, void* U_, const PointSrcArgs& 
 // PointSource.propagate_to without Fresnel scaling (big-wave/source.py:97-107).
 int rs_point_source_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double xs,
                               double ys, double z, double wl, double cutoff, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan(p));
   if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
   PointSrcArgs a{};
@@ -982,6 +1244,7 @@ int rs_point_source_propagate(rs_plan* p, void* u_, void* U_, double dx, double 
 // Fresnel-scaled source plane (big-wave/source.py:62-95).
 int rs_fresnel_plane(rs_plan* p, void* u, double dx, double dy, double xs, double ys, double dz, double wl,
                      void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan(p));
   if (!u) return fail(RS_EINVAL, "NULL field pointer");
   if (!(dz > 0.0) || !std::isfinite(dz)) return fail(RS_EINVAL, "Fresnel source-to-sample distance must be positive");
@@ -995,6 +1258,7 @@ int rs_fresnel_plane(rs_plan* p, void* u, double dx, double dy, double xs, doubl
 
 int rs_fresnel_plane_propagate(rs_plan* p, void* u_, void* U_, double dx, double dy, double xs, double ys,
                                double dz, double wl, double cutoff, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_fresnel_plane_propagate"));
   if (!u_ || !U_) return fail(RS_EINVAL, "NULL field pointer");
   if (!(dz > 0.0) || !std::isfinite(dz)) return fail(RS_EINVAL, "Fresnel source-to-sample distance must be positive");
@@ -1037,6 +1301,7 @@ int rs_multislice_voxel(rs_plan* p, void* u, void* U, const void* grid, int grid
                         int n_db, const rs_voxel_geom* geom, double dx, double dy, double wl,
                         double cutoff, const double* slice_dz, const double* coord_scale,
                         int slice_begin, int slice_end, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_multislice_voxel"));
   if (!grid || !db) return fail(RS_EINVAL, "grid and db must be device pointers");
   if (n_db < 1) return fail(RS_EINVAL, "n_db must be >= 1");
@@ -1053,6 +1318,7 @@ int rs_multislice_voxel_stacked(rs_plan* p, int batch, void* u, void* U, const v
                                 const float* db, int n_db, const rs_voxel_geom* geom, double dx, double dy,
                                 double wl, double cutoff, const double* slice_dz, const double* coord_scale,
                                 int slice_begin, int slice_end, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_multislice_voxel_stacked"));
   if (!grid || !db) return fail(RS_EINVAL, "grid and db must be device pointers");
   if (n_db < 1) return fail(RS_EINVAL, "n_db must be >= 1");
@@ -1072,6 +1338,7 @@ int rs_multislice_plasma(rs_plan* p, void* u, void* U, const void* ne, const voi
                          const rs_voxel_geom* geom, double dx, double dy, double wl, double cutoff,
                          const double* slice_dz, const double* coord_scale, int slice_begin,
                          int slice_end, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_multislice_plasma"));
   if (!ne || !ni || !te || !zstar) return fail(RS_EINVAL, "plasma grids must be device pointers");
   if (!pc || !finite_pos(pc->energy_ev)) return fail(RS_EINVAL, "energy must be positive");
@@ -1101,6 +1368,7 @@ int rs_multislice_plasma(rs_plan* p, void* u, void* U, const void* ne, const voi
 int rs_multislice_dbgrid(rs_plan* p, void* u, void* U, const float* db_grid, const rs_voxel_geom* geom,
                          double dx, double dy, double wl, double cutoff, const double* slice_dz,
                          const double* coord_scale, int slice_begin, int slice_end, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_multislice_dbgrid"));
   if (!db_grid) return fail(RS_EINVAL, "db_grid must be a device pointer");
   SliceSource src;
@@ -1114,6 +1382,7 @@ int rs_multislice_dbgrid_store(rs_plan* p, void* u, void* U, const float* db_gri
                                double dx, double dy, double wl, double cutoff, const double* slice_dz,
                                const double* coord_scale, int slice_begin, int slice_end, void* fields,
                                void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_multislice_dbgrid_store"));
   if (!db_grid || !fields) return fail(RS_EINVAL, "db_grid and fields must be device pointers");
   if (!p->fast) return fail(RS_EUNSUPPORTED, "field storing needs the fused passes (fast sizes)");
@@ -1129,6 +1398,7 @@ int rs_adjoint_multislice_dbgrid(rs_plan* p, void* g, const float* db_grid, cons
                                  double dy, double wl, double cutoff, const double* slice_dz,
                                  const double* coord_scale, int slice_begin, int slice_end, const void* fields,
                                  float* grad_grid, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_adjoint_multislice_dbgrid"));
   if (!g || !db_grid || !fields || !grad_grid || !geom || !slice_dz) return fail(RS_EINVAL, "NULL pointer argument");
   if (geom->nz <= 0 || geom->ny_v < 2 || geom->nx_v < 2) return fail(RS_EINVAL, "bad grid shape");
@@ -1186,6 +1456,7 @@ int rs_adjoint_multislice_dbgrid(rs_plan* p, void* g, const float* db_grid, cons
 int rs_adjoint_slice(rs_plan* p, void* v, const void* u, const float* db_grid, const rs_voxel_geom* g,
                      double dx, double dy, double wl, int slice, double coord_scale, float* grad_grid,
                      void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_adjoint_slice"));
   if (!v || !u || !db_grid || !grad_grid || !g) return fail(RS_EINVAL, "NULL pointer argument");
   if (slice < 0 || slice >= g->nz) return fail(RS_EINVAL, "slice %d outside [0, %d)", slice, g->nz);
@@ -1268,14 +1539,7 @@ int rs_detector_adjoint(rs_plan* p, const void* u, void* g_out, const double* r,
   put(o_ydet, ydet.data(), ydet.size() * 4);
   cudaStream_t s = as_stream(stream);
   p->det_cache.valid = false;  // the buffer now holds the transposed tables
-  if (total > p->det_cap) {
-    if (p->det) RS_CK(cudaFree(p->det));
-    p->det = nullptr;
-    p->det_cap = 0;
-    cudaError_t e = cudaMalloc(&p->det, total);
-    if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc(%zu) for detector tables: %s", total, cudaGetErrorString(e));
-    p->det_cap = total;
-  }
+  RS_TRY(grow_det(p, total));
   char* d = static_cast<char*>(p->det);
   RS_CK(cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, s));
   DetAdjArgs a{};
@@ -1301,6 +1565,7 @@ int rs_detector_adjoint(rs_plan* p, const void* u, void* g_out, const double* r,
 int rs_apply_transmission_voxel(rs_plan* p, void* u, const void* grid, int grid_signed, const float* db,
                                 int n_db, const rs_voxel_geom* g, double dx, double dy, double wl,
                                 int slice, double coord_scale, void* stream) {
+  StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_apply_transmission_voxel"));
   if (!u || !grid || !db || !g) return fail(RS_EINVAL, "NULL pointer argument");
   if (slice < 0 || slice >= g->nz) return fail(RS_EINVAL, "slice %d outside [0, %d)", slice, g->nz);
@@ -1339,15 +1604,7 @@ int rs_detector(rs_plan* p, const void* u, double* out, const rs_detector_geom* 
     if (g->integrator == 0) build_area_v1(p->nx, p->ny, *g, t);
     else build_legacy(p->nx, p->ny, *g, t);
     size_t* o = dc.off;
-    o[0] = 0;                                     // xdet
-    o[1] = o[0] + align8(t.xdet.size() * 8);      // ydet
-    o[2] = o[1] + align8(t.ydet.size() * 8);      // yw
-    o[3] = o[2] + align8(t.yw.size() * 8);        // xw
-    o[4] = o[3] + align8(t.xw.size() * 4);        // xptr
-    o[5] = o[4] + align8(t.xptr.size() * 4);      // xcell
-    o[6] = o[5] + align8(t.xcell.size() * 4);     // yptr
-    o[7] = o[6] + align8(t.yptr.size() * 4);      // ycell
-    const size_t total = o[7] + align8(t.ycell.size() * 4) + 8;
+    const size_t total = det_layout(t, o);
     std::vector<char> host(total, 0);
     auto put = [&](size_t off, const void* src, size_t n) { if (n) std::memcpy(host.data() + off, src, n); };
     put(o[0], t.xdet.data(), t.xdet.size() * 8);
@@ -1358,14 +1615,7 @@ int rs_detector(rs_plan* p, const void* u, double* out, const rs_detector_geom* 
     put(o[5], t.xcell.data(), t.xcell.size() * 4);
     put(o[6], t.yptr.data(), t.yptr.size() * 4);
     put(o[7], t.ycell.data(), t.ycell.size() * 4);
-    if (total > p->det_cap) {
-      if (p->det) RS_CK(cudaFree(p->det));  // cudaFree waits for work still using the old buffer
-      p->det = nullptr;
-      p->det_cap = 0;
-      cudaError_t e = cudaMalloc(&p->det, total);
-      if (e != cudaSuccess) return fail(RS_ENOMEM, "cudaMalloc(%zu) for detector tables: %s", total, cudaGetErrorString(e));
-      p->det_cap = total;
-    }
+    RS_TRY(grow_det(p, total));
     // Pageable host->device copies are staged before cudaMemcpyAsync returns, so `host` may be
     // released now; the kernel is ordered after the copy on the same stream.
     RS_CK(cudaMemcpyAsync(p->det, host.data(), total, cudaMemcpyHostToDevice, s));
@@ -1406,8 +1656,7 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 
 constexpr int kMaxDevices = 64;
 void* g_noalloc_addr[kMaxDevices] = {};
-std::once_flag g_noalloc_once[kMaxDevices];
-cudaError_t g_noalloc_setup_err[kMaxDevices] = {};
+std::mutex g_noalloc_mu;  // guards the look-up; only a successful address is kept
 
 }  // namespace
 
@@ -1422,16 +1671,21 @@ extern "C" int rs_detector_noalloc(const void* u, int nx, int ny, double* out, c
   int dev = -1;
   RS_CK(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kMaxDevices) return fail(RS_EUNSUPPORTED, "device ordinal %d above %d", dev, kMaxDevices - 1);
-  // Once per device, with that device current: the device address of the scratch array (the
-  // host-side symbol is only a stand-in and must never reach a kernel).
-  std::call_once(g_noalloc_once[dev], [dev] {
-    void* ptr = nullptr;
-    g_noalloc_setup_err[dev] = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-    g_noalloc_addr[dev] = ptr;
-  });
-  if (g_noalloc_setup_err[dev] != cudaSuccess || !g_noalloc_addr[dev])
-    return fail(RS_ECUDA, "cudaGetSymbolAddress of the detector scratch failed: %s",
-                cudaGetErrorString(g_noalloc_setup_err[dev]));
+  // Per device, with that device current: the device address of the scratch array (the
+  // host-side symbol is only a stand-in and must never reach a kernel). A failed look-up (e.g. one
+  // made during a stream capture) is not remembered: the next call tries again.
+  void* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+      void* ptr = nullptr;
+      const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+      if (e != cudaSuccess || !ptr)
+        return fail(RS_ECUDA, "cudaGetSymbolAddress of the detector scratch failed: %s", cudaGetErrorString(e));
+      g_noalloc_addr[dev] = ptr;
+    }
+    scratch = g_noalloc_addr[dev];
+  }
   DetTables t;
   if (g->integrator == 0) build_area_v1(nx, ny, *g, t);
   else if (g->integrator == 1) build_legacy(nx, ny, *g, t);
@@ -1461,7 +1715,7 @@ extern "C" int rs_detector_noalloc(const void* u, int nx, int ny, double* out, c
   put(o_yptr, t.yptr.data(), t.yptr.size() * 4);
   put(o_ycell, t.ycell.data(), t.ycell.size() * 4);
   cudaStream_t s = as_stream(stream);
-  char* d = static_cast<char*>(g_noalloc_addr[dev]);
+  char* d = static_cast<char*>(scratch);
   // Every entry the kernel reads is rewritten here, so nothing left by an earlier call is used.
   RS_CK(cudaMemcpyAsync(d, host.data(), total, cudaMemcpyHostToDevice, s));
   DetArgs a{};

@@ -1,0 +1,300 @@
+// rs_fft2x.cuh — the register-resident Stockham FFT of rs_fft.cuh for two sequences at once,
+// in split (structure-of-arrays) form, with dithered twiddle tables. Used by the multislice
+// passes (rs_x2.cuh); the other entry points keep rs_fft.cuh.
+//
+// Split form. A thread holds the same positions of two sequences A and B (two rows, or the two
+// columns of a strip): value e is cp2{re = (Re A_e, Re B_e), im = (Im A_e, Im B_e)}. Every
+// complex add, subtract or product is then two packed f32x2 instructions that touch no operand
+// twice, where the interleaved (re, im) form needs register moves and negations to build the
+// packed operands, and each twiddle is loaded once for both sequences. Multiplications by -i
+// inside the butterflies are folded into the adds and subtracts that consume them.
+//
+// Dithered twiddles. A twiddle (or DFT constant) rounded to float applies the same relative
+// error (~3e-8) to every transform of every slice, so over hundreds of slices the errors add up
+// coherently. The compensated tables of rs_fft.cuh remove that error with two extra products per
+// value. Here instead each table entry is one of the two floats that bracket the exact value, and
+// the plan keeps kDitherTables tables in which the upper neighbour is used in a fraction of the
+// tables equal to the exact value's position between the two (to 1/2K of an ulp). Slice k of a run
+// uses table k mod K, so the error a slice makes differs from slice to slice and its mean over
+// K slices is zero to 1/(2K) ulp; a float32 emulation of 514 slices at K = 64 gives the same
+// intensity error as exact twiddles (1.05e-5 vs 1.06e-5; 7.4e-5 with fixed rounded twiddles).
+// A table entry holds its twiddle as (wr, wr, wi, wi): both sequences' multiplier pairs.
+#pragma once
+#include "rs_fft.cuh"
+
+namespace rs {
+
+constexpr int kDitherTables = 64;
+
+struct __align__(16) cp2 {
+  float2 re, im;
+};
+
+__device__ __forceinline__ float2 p_add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 p_mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 p_fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+// a - b as one fused multiply-add b * (-1) + a (exact negation, one rounding: the subtraction)
+__device__ __forceinline__ float2 p_sub(float2 a, float2 b) { return __ffma2_rn(b, make_float2(-1.f, -1.f), a); }
+
+__device__ __forceinline__ cp2 x_add(cp2 a, cp2 b) { return {p_add(a.re, b.re), p_add(a.im, b.im)}; }
+__device__ __forceinline__ cp2 x_sub(cp2 a, cp2 b) { return {p_sub(a.re, b.re), p_sub(a.im, b.im)}; }
+// a + r*b and a - r*b with r = -i (forward) or +i (inverse): -i*b = (b.im, -b.re), +i*b = (-b.im, b.re)
+template <bool INV>
+__device__ __forceinline__ cp2 x_add_rot(cp2 a, cp2 b) {
+  return INV ? cp2{p_sub(a.re, b.im), p_add(a.im, b.re)} : cp2{p_add(a.re, b.im), p_sub(a.im, b.re)};
+}
+template <bool INV>
+__device__ __forceinline__ cp2 x_sub_rot(cp2 a, cp2 b) {
+  return INV ? cp2{p_add(a.re, b.im), p_sub(a.im, b.re)} : cp2{p_sub(a.re, b.im), p_add(a.im, b.re)};
+}
+// a * (wr + i wi) given the pairs WR = (wr, wr), WI = (wi, wi) and NWI = -WI:
+// re = fma(re, wr, im * -wi), im = fma(im, wr, re * wi)
+__device__ __forceinline__ cp2 x_mul3(cp2 a, float2 wr, float2 wi, float2 nwi) {
+  return {p_fma(a.re, wr, p_mul(a.im, nwi)), p_fma(a.im, wr, p_mul(a.re, wi))};
+}
+// Per-lane product a * h, h = (HR, HI) holding a different multiplier for each sequence.
+__device__ __forceinline__ cp2 x_mul_pair(cp2 a, cp2 h) {
+  const float2 nhi = p_sub(make_float2(0.f, 0.f), h.im);
+  return {p_fma(a.re, h.re, p_mul(a.im, nhi)), p_fma(a.im, h.re, p_mul(a.re, h.im))};
+}
+// Table twiddle w = (wr, wr, wi, wi): forward a * w, inverse a * conj(w).
+template <bool INV>
+__device__ __forceinline__ cp2 x_mul_tw(cp2 a, float4 w) {
+  const float2 wr = make_float2(w.x, w.y), wi = make_float2(w.z, w.w);
+  const float2 nwi = p_sub(make_float2(0.f, 0.f), wi);
+  return INV ? x_mul3(a, wr, nwi, wi) : x_mul3(a, wr, wi, nwi);
+}
+
+// The real constants of the small DFTs for one table of a run: cos(pi/8), sin(pi/8) and
+// sqrt(2)/2, each dithered like the twiddle tables (host-built, one set per table).
+struct DftConsts {
+  float c8, s8, r2;
+};
+struct DftK {
+  float2 c8, nc8, s8, ns8, r2, nr2;
+};
+__device__ __forceinline__ DftK dft_k(const DftConsts& k) {
+  return {make_float2(k.c8, k.c8), make_float2(-k.c8, -k.c8), make_float2(k.s8, k.s8),
+          make_float2(-k.s8, -k.s8), make_float2(k.r2, k.r2), make_float2(-k.r2, -k.r2)};
+}
+
+// Multiply by W16^M = exp(-+2 pi i M/16) (M as used inside the radix-16 butterfly; M = 4 is
+// folded into the butterfly's adds).
+template <int M, bool INV>
+__device__ __forceinline__ cp2 tw16x(cp2 a, const DftK& k) {
+  if constexpr (M == 0) {
+    return a;
+  } else if constexpr (M == 2) {
+    // forward r2 (1 - i): r2 (re + im, im - re); inverse r2 (1 + i): r2 (re - im, re + im)
+    return INV ? cp2{p_mul(p_sub(a.re, a.im), k.r2), p_mul(p_add(a.re, a.im), k.r2)}
+               : cp2{p_mul(p_add(a.re, a.im), k.r2), p_mul(p_sub(a.im, a.re), k.r2)};
+  } else if constexpr (M == 6) {
+    // forward r2 (-1 - i): (r2 (im - re), -r2 (re + im)); inverse r2 (-1 + i): (-r2 (re + im), r2 (re - im))
+    return INV ? cp2{p_mul(p_add(a.re, a.im), k.nr2), p_mul(p_sub(a.re, a.im), k.r2)}
+               : cp2{p_mul(p_sub(a.im, a.re), k.r2), p_mul(p_add(a.re, a.im), k.nr2)};
+  } else if constexpr (M == 1) {  // forward (c8, -s8)
+    return INV ? x_mul3(a, k.c8, k.s8, k.ns8) : x_mul3(a, k.c8, k.ns8, k.s8);
+  } else if constexpr (M == 3) {  // forward (s8, -c8)
+    return INV ? x_mul3(a, k.s8, k.c8, k.nc8) : x_mul3(a, k.s8, k.nc8, k.c8);
+  } else {
+    static_assert(M == 9, "W16 power");  // forward (-c8, s8)
+    return INV ? x_mul3(a, k.nc8, k.ns8, k.s8) : x_mul3(a, k.nc8, k.s8, k.ns8);
+  }
+}
+
+// 4-point DFT in place; ROT2: a2 arrives still to be multiplied by -i (forward) / +i (inverse).
+template <bool INV, bool ROT2 = false>
+__device__ __forceinline__ void dft4x(cp2& a0, cp2& a1, cp2& a2, cp2& a3) {
+  const cp2 t0 = ROT2 ? x_add_rot<INV>(a0, a2) : x_add(a0, a2);
+  const cp2 t1 = ROT2 ? x_sub_rot<INV>(a0, a2) : x_sub(a0, a2);
+  const cp2 t2 = x_add(a1, a3);
+  const cp2 d = x_sub(a1, a3);
+  a0 = x_add(t0, t2);
+  a2 = x_sub(t0, t2);
+  a1 = x_add_rot<INV>(t1, d);
+  a3 = x_sub_rot<INV>(t1, d);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft2x(cp2& a0, cp2& a1) {
+  const cp2 t = a0;
+  a0 = x_add(t, a1);
+  a1 = x_sub(t, a1);
+}
+
+// Natural order in and out.
+template <bool INV>
+__device__ __forceinline__ void dft8x(cp2 (&a)[8], const DftK& k) {
+  dft4x<INV>(a[0], a[2], a[4], a[6]);
+  dft4x<INV>(a[1], a[3], a[5], a[7]);
+  a[3] = tw16x<2, INV>(a[3], k);  // W8^1
+  a[7] = tw16x<6, INV>(a[7], k);  // W8^3; W8^2 of a[5] folded below
+  cp2 y[8];
+  y[0] = x_add(a[0], a[1]);
+  y[4] = x_sub(a[0], a[1]);
+  y[1] = x_add(a[2], a[3]);
+  y[5] = x_sub(a[2], a[3]);
+  y[2] = x_add_rot<INV>(a[4], a[5]);
+  y[6] = x_sub_rot<INV>(a[4], a[5]);
+  y[3] = x_add(a[6], a[7]);
+  y[7] = x_sub(a[6], a[7]);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) a[i] = y[i];
+}
+
+// 16-point DFT as 4 x 4 (as dft16 of rs_common.cuh), natural order in and out.
+template <bool INV>
+__device__ __forceinline__ void dft16x(cp2 (&a)[16], const DftK& k) {
+#pragma unroll
+  for (int r2 = 0; r2 < 4; ++r2) dft4x<INV>(a[r2], a[4 + r2], a[8 + r2], a[12 + r2]);
+  a[5] = tw16x<1, INV>(a[5], k);
+  a[9] = tw16x<2, INV>(a[9], k);
+  a[13] = tw16x<3, INV>(a[13], k);
+  a[6] = tw16x<2, INV>(a[6], k);
+  a[14] = tw16x<6, INV>(a[14], k);  // a[10] (W16^4) folded into its row butterfly
+  a[7] = tw16x<3, INV>(a[7], k);
+  a[11] = tw16x<6, INV>(a[11], k);
+  a[15] = tw16x<9, INV>(a[15], k);
+  dft4x<INV>(a[0], a[1], a[2], a[3]);
+  dft4x<INV>(a[4], a[5], a[6], a[7]);
+  dft4x<INV, true>(a[8], a[9], a[10], a[11]);
+  dft4x<INV>(a[12], a[13], a[14], a[15]);
+  cp2 y[16];
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) y[k1 + 4 * k2] = a[4 * k1 + k2];
+#pragma unroll
+  for (int i = 0; i < 16; ++i) a[i] = y[i];
+}
+
+template <int R, bool INV, int OFF>
+__device__ __forceinline__ void dft_slice2x(cp2 (&v)[16], const DftK& k) {
+  if constexpr (R == 16) {
+    static_assert(OFF == 0, "radix-16 stages use the whole array");
+    dft16x<INV>(v, k);
+  } else if constexpr (R == 8) {
+    cp2 a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = v[OFF + i];
+    dft8x<INV>(a, k);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) v[OFF + i] = a[i];
+  } else if constexpr (R == 4) {
+    dft4x<INV>(v[OFF], v[OFF + 1], v[OFF + 2], v[OFF + 3]);
+  } else if constexpr (R == 2) {
+    dft2x<INV>(v[OFF], v[OFF + 1]);
+  }
+}
+
+template <int R, bool INV, int... Bs>
+__device__ __forceinline__ void dft_all2x(cp2 (&v)[16], const DftK& k, std::integer_sequence<int, Bs...>) {
+  (dft_slice2x<R, INV, Bs * R>(v, k), ...);
+}
+
+// Stockham stages of FftPlan<N> (powers of two: 16 values per thread) on split pairs; the same
+// stage structure, register mappings and exchange addressing as FftStages, with the exchange
+// buffer holding one cp2 (16 bytes) per position. tw: this table's stage-major dithered entries.
+template <int N, bool INV, int SI, int NS, class AD = PadAddr, bool WARP = false, class TWL = TwGlobal, int STR = 1>
+struct FftStages2x {
+  using P = FftPlan<N>;
+  static_assert(P::POW2, "split-pair transforms are built for power-of-two lengths");
+  static __device__ __forceinline__ void run(cp2 (&v)[16], cp2* buf, int t, const float4* __restrict__ tw,
+                                             const DftK& k) {
+    constexpr int R = P::radix(INV, SI);
+    constexpr int B = 16 / R;
+    constexpr int T = P::T;
+    if constexpr (NS > 1) {
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int kk = (t + b * T) % NS;
+        constexpr int TW_OFF = (INV ? P::INV_BASE : 0) + P::stage_offset(INV, SI);
+        const float4* tws = tw + TW_OFF + kk;
+#pragma unroll
+        for (int r = 1; r < R; ++r) v[b * R + r] = x_mul_tw<INV>(v[b * R + r], TWL::load(&tws[(r - 1) * NS]));
+      }
+    }
+    dft_all2x<R, INV>(v, k, std::make_integer_sequence<int, B>{});
+    if constexpr (SI + 1 < P::NST) {
+      constexpr int R2 = P::radix(INV, SI + 1);
+      if constexpr (WARP) __syncwarp();
+#pragma unroll
+      for (int b = 0; b < B; ++b) {
+        const int j = t + b * T;
+        const int base = (j / NS) * NS * R + (j % NS);
+        const int pb = AD::at(base);
+#pragma unroll
+        for (int q = 0; q < R; ++q) buf[AD::at_plus(base, pb, q * NS, NS == 1 && R % 16 == 0) * STR] = v[b * R + q];
+      }
+      if constexpr (WARP) __syncwarp(); else __syncthreads();
+      const int pt = AD::at(t);
+#pragma unroll
+      for (int e = 0; e < 16; ++e) v[e] = buf[AD::at_plus(t, pt, slot_pos<N, R2>(0, e), false) * STR];
+      if constexpr (!WARP) __syncthreads();
+      FftStages2x<N, INV, SI + 1, NS * R, AD, WARP, TWL, STR>::run(v, buf, t, tw, k);
+    }
+  }
+};
+
+template <int N, bool INV, class AD = PadAddr, class TWL = TwGlobal>
+__device__ __forceinline__ void fft_seq2x(cp2 (&v)[16], cp2* buf, int t, const float4* __restrict__ tw,
+                                          const DftK& k) {
+  FftStages2x<N, INV, 0, 1, AD, false, TWL>::run(v, buf, t, tw, k);
+}
+
+// Barrier of the threads that share one transform's block exchange: the whole block, or one
+// named group of `count` threads (barrier `id` > 0) when a block runs independent groups.
+struct BarBlock {
+  __device__ __forceinline__ void sync() const { __syncthreads(); }
+};
+struct BarGroup {
+  int id, count;
+  __device__ __forceinline__ void sync() const { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
+};
+
+// Two-level transform of Fft2L<N> on split pairs (the same steps and mappings as fft2l_fwd /
+// fft2l_inv); table: W_N^{c m} at (c-1)*T + m, then the T-point stage-major table.
+template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock>
+__device__ __forceinline__ void fft2l_fwd2x(cp2 (&v)[16], cp2* buf, int t, const float4* __restrict__ tw,
+                                            const DftK& k, const BAR& bar = BAR{}) {
+  using F = Fft2L<N>;
+  constexpr int T = F::T;
+  constexpr int G = F::G;
+  dft16x<false>(v, k);
+#pragma unroll
+  for (int c = 1; c < 16; ++c) v[c] = x_mul_tw<false>(v[c], TWL::load(&tw[(c - 1) * T + t]));
+  const int pt = BX::at(t);
+#pragma unroll
+  for (int c = 0; c < 16; ++c) buf[BX::at_plus(t, pt, c * T, false) * STR] = v[c];
+  bar.sync();
+  const int c = t / G;
+  const int j = t % G;
+  const int pg = BX::at(c * T + j);
+#pragma unroll
+  for (int e = 0; e < 16; ++e) v[e] = buf[BX::at_plus(c * T + j, pg, e * G, false) * STR];
+  FftStages2x<T, false, 0, 1, AD, true, TWL, STR>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
+}
+
+template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock>
+__device__ __forceinline__ void fft2l_inv2x(cp2 (&v)[16], cp2* buf, int t, const float4* __restrict__ tw,
+                                            const DftK& k, const BAR& bar = BAR{}) {
+  using F = Fft2L<N>;
+  constexpr int T = F::T;
+  constexpr int G = F::G;
+  const int c = t / G;
+  const int j = t % G;
+  FftStages2x<T, true, 0, 1, AD, true, TWL, STR>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
+  __syncwarp();
+  const int pg = BX::at(c * T + j);
+#pragma unroll
+  for (int e = 0; e < 16; ++e) buf[BX::at_plus(c * T + j, pg, e * G, false) * STR] = v[e];
+  bar.sync();
+  const int pt = BX::at(t);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) v[q] = buf[BX::at_plus(t, pt, q * T, false) * STR];
+#pragma unroll
+  for (int q = 1; q < 16; ++q) v[q] = x_mul_tw<true>(v[q], TWL::load(&tw[(q - 1) * T + t]));
+  dft16x<true>(v, k);
+}
+
+}  // namespace rs

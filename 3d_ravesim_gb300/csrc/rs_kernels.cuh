@@ -7,7 +7,7 @@
 // after the transmission multiply of big-wave/optical_element.py:565-584). Both passes read
 // their whole row / column strip into registers before writing, so they run in place.
 #pragma once
-#include "rs_fft.cuh"
+#include "rs_fft2x.cuh"
 
 namespace rs {
 
@@ -85,6 +85,11 @@ struct RowArgs {
   float2* aux;           // ROW_STORE_U: the fields entering the slice; adjoint: read from here
   float* grad;           // adjoint: dL/d(delta, beta) of the slice, float pairs per voxel
   int axis_rows;         // stacked fields: rows per field (the y tables repeat); 0 = ny
+  // split-pair passes (row_x2_kernel): this slice's dithered tables and DFT constants for the
+  // inverse and the forward transform
+  const float4* twd_inv;
+  const float4* twd_fwd;
+  DftConsts k_inv, k_fwd;
 };
 
 struct ColArgs {
@@ -112,9 +117,32 @@ struct ColArgs {
   int tw4;
   int tw4q;
   const float4* tw4t;
+  // Test hook of the pipelined pass: wait (with a short bound) on a barrier that nothing completes,
+  // record the timeout in the status word and return before any copy is issued.
+  int test_stall;
+  // split-pair column pass (col_x2_pipe_kernel): this slice's dithered two-level table and constants
+  const float4* twd;
+  DftConsts kc;
 };
 
 // ----------------------------------------------------------------------------- physics
+// sin(pi h) and cos(pi h). For |h| < 1/16 (|pi h| < 0.2, the usual thin-slice half angle) by
+// their Taylor series through x^9 and x^8 (first omitted terms below 5e-16 and 3e-14 of the
+// result) with x = pi h formed from a two-float pi; otherwise sincospif.
+constexpr float kPiHi = 3.14159274101257324219f;
+constexpr float kPiLo = -8.74227766e-08f;
+__device__ __forceinline__ void sincospi_small(float h, float* s, float* c) {
+  if (fabsf(h) < 0.0625f) {
+    const float x = fmaf(h, kPiHi, h * kPiLo);
+    const float x2 = x * x;
+    *s = x * fmaf(x2, fmaf(x2, fmaf(x2, fmaf(x2, 2.7557319e-06f, -1.9841270e-04f), 8.3333333e-03f),
+                           -1.6666667e-01f), 1.0f);
+    *c = fmaf(x2, fmaf(x2, fmaf(x2, fmaf(x2, 2.4801587e-05f, -1.3888889e-03f), 4.1666667e-02f), -0.5f), 1.0f);
+  } else {
+    sincospif(h, s, c);
+  }
+}
+
 __device__ __forceinline__ float2 material_factor(float delta, float beta, float a) {
   // exp(-2*pi*i*a*conj(delta + i*beta)) = exp(-2*pi*a*beta) * exp(-2*pi*i*a*delta)
   // (big-wave/optical_element.py:39-42)
@@ -123,7 +151,7 @@ __device__ __forceinline__ float2 material_factor(float delta, float beta, float
   // unbiased one to nearest: cos(phi) = 1 - 2 sin^2(phi/2), sin(phi) = 2 sin(phi/2) cos(phi/2)
   // from the half angle phi/2 = pi*a*delta, and exp(x) = 1 + expm1(x).
   float sh, ch;
-  sincospif(a * delta, &sh, &ch);
+  sincospi_small(a * delta, &sh, &ch);
   const float c = fmaf(-2.0f * sh, sh, 1.0f);
   const float s = 2.0f * sh * ch;
   const float x = -6.283185307179586f * a * beta;

@@ -19,6 +19,7 @@
 namespace rs {
 
 constexpr uint32_t kSpinLimit = 1u << 22;
+constexpr uint32_t kTestSpinLimit = 1u << 14;  // the test hook's wait (ColArgs::test_stall)
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -43,8 +44,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return done != 0;
 }
 // Bounded wait; returns false (and records the failure) when the copy never landed.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* status,
+                                                  uint32_t limit = kSpinLimit) {
+  for (uint32_t i = 0; i < limit; ++i)
     if (mbar_try_wait(bar, parity)) return true;
   if (status) atomicExch(status, 1);
   return false;
@@ -318,6 +320,12 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
     fence_mbar_init();
   }
   __syncthreads();
+  if (a.test_stall) {
+    // Phase 0 of a fresh barrier completes only on an arrival, and none is made: every thread's
+    // bounded wait runs out, the status word records it, and the block returns with no copy issued.
+    mbar_wait_bounded(&bars[0], 0, status, kTestSpinLimit);
+    return;
+  }
 
   const float4* tw_g = G::L2 ? a.tw2 : a.tw;
   if constexpr (G::TW_SMEM) {  // the block's copy of the twiddle tables (read from L2 once)

@@ -1,0 +1,16 @@
+// rs_x2_api.cuh — host entry points of the split-pair multislice passes (rs_pass_x2.cu).
+#pragma once
+#include <cuda.h>
+
+#include "rs_kernels.cuh"
+
+namespace rs {
+bool row_x2_ok(int nx);
+int row_x2_slots(int nx);
+bool col_x2_box(int ny, int* w, int* bh);
+cudaError_t launch_row_x2(int nx, const RowArgs& a, cudaStream_t s);
+cudaError_t launch_col_x2(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
+                          cudaStream_t s);
+// kDitherTables dithered copies of a compensated table of `len` entries (rs_fft2x.cuh)
+cudaError_t launch_dither_tables(const float4* comp, float4* out, int len, cudaStream_t s);
+}  // namespace rs

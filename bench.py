@@ -173,11 +173,18 @@ def l2_flush_buffer(torch, device):
 
 def schedule_name(mask: int) -> str:
     """Readable form of a pass-schedule mask (bits: 1 pipelined rows, 2 pipelined columns,
-    4 general row kernel, 8 split columns)."""
-    rows = "rows:pipelined" if mask & 1 else ("rows:per-block" if mask & 4 else "rows:per-block-voxel")
-    cols = "cols:pipelined" if mask & 2 else "cols:per-block"
-    if mask & 8:
-        cols = "cols:split-3-pass (last slice " + cols.split(":")[1] + ")"
+    4 general row kernel, 8 split columns, 16 / 32 single-sequence compensated rows / columns
+    instead of the split-pair passes, for the sizes that have them)."""
+    if mask & 16:
+        rows = "rows:pipelined" if mask & 1 else ("rows:per-block" if mask & 4 else "rows:per-block-voxel")
+    else:
+        rows = "rows:split-pair"
+    if mask & 32:
+        cols = "cols:pipelined" if mask & 2 else "cols:per-block"
+        if mask & 8:
+            cols = "cols:split-3-pass (last slice " + cols.split(":")[1] + ")"
+    else:
+        cols = "cols:split-pair"
     return f"{rows},{cols}"
 
 

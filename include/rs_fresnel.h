@@ -244,17 +244,53 @@ int rs_plan_set_pipeline(rs_plan* plan, int mask);
  *                        from the single pass at the FP32 level (the other bits reproduce it
  *                        exactly).
  * rs_plan_schedules lists the masks that are distinct for the plan's sizes (it writes at most
- * `cap` of them and the total to *count). No reference function: big-wave has one FFT schedule. */
+ * `cap` of them and the total to *count). Where the split-pair passes run (no
+ * RS_SCHED_COMPENSATED), the bits that pick among the single-sequence kernels of that direction
+ * are not listed. No reference function: big-wave has one FFT schedule. */
 #define RS_SCHED_PIPE_ROWS 1
 #define RS_SCHED_PIPE_COLS 2
 #define RS_SCHED_ROW_GENERAL 4
 #define RS_SCHED_SPLIT_COLS 8
+/*   RS_SCHED_COMP_ROWS,  the multislice row (resp. column) passes run the single-sequence kernels
+ *   RS_SCHED_COMP_COLS   with compensated (float + residual) twiddles, as every other entry point
+ *                        does, instead of the split-pair passes: two rows (or two columns) per
+ *                        thread group in packed f32x2 arithmetic with 64 dithered twiddle tables,
+ *                        slice k using table k mod 64 (their rounding errors average out over
+ *                        slices instead of adding up). Both keep the FP64-vs-FP32 intensity error of
+ *                        a 514-slice run within 2e-5; their results differ at the FP32 rounding level. */
+#define RS_SCHED_COMP_ROWS 16
+#define RS_SCHED_COMP_COLS 32
+#define RS_SCHED_COMPENSATED (RS_SCHED_COMP_ROWS | RS_SCHED_COMP_COLS)
 int rs_plan_set_schedule(rs_plan* plan, int mask);
 int rs_plan_get_schedule(const rs_plan* plan, int* mask);
 int rs_plan_schedules(const rs_plan* plan, int* masks, int cap, int* count);
 /* Synchronises the device and returns the plan's device status word: 0, or non-zero (with
  * RS_ETIMEOUT) if a pipelined pass gave up waiting for a bulk copy. */
 int rs_plan_status(rs_plan* plan, int* device_status);
+/* The same answer without a device synchronisation: every call that ran a pipelined pass queues
+ * a 4-byte copy of the status word into pinned host memory on its stream, so once the caller has
+ * synchronised that stream (as it does to read a detector image) this reads the word as of its
+ * last call. Returns RS_ETIMEOUT when it is set: the field that pass wrote is not valid. A status
+ * stays set until rs_plan_clear_status (which synchronises `stream`). No reference counterpart:
+ * big-wave's NumPy path has no device waits. */
+int rs_plan_check(const rs_plan* plan, int* device_status);
+int rs_plan_clear_status(rs_plan* plan, void* stream);
+/* Test hook: the next pipelined column pass of the plan waits (with a short bound, about 2^14
+ * polls) on a barrier that nothing completes, records the timeout in the status word and returns
+ * without touching the field, as a pass whose bulk copy never landed would. One-shot. */
+int rs_plan_test_stall(rs_plan* plan, int enable);
+
+/* Buffers that grow with the geometry: the detector tables of rs_detector and the plasma slice
+ * plane of rs_multislice_plasma. Growing one mid-run frees and reallocates device memory (and
+ * so synchronises the device); a caller that knows its run reserves both first.
+ * rs_detector_table_bytes gives the table bytes rs_detector needs for a geometry (host only);
+ * rs_plan_reserve grows the buffers to at least the given sizes now. rs_alloc_count returns the
+ * number of device and pinned-host allocations this library has made in the process (plans,
+ * tables, status words), so a caller can check that a run allocated nothing.
+ * Reference counterpart: none (big-wave allocates NumPy arrays per call). */
+int rs_detector_table_bytes(int nx, int ny, const rs_detector_geom* geom, size_t* bytes);
+int rs_plan_reserve(rs_plan* plan, size_t detector_table_bytes, size_t plasma_plane_voxels);
+int rs_alloc_count(unsigned long long* out);
 
 /* Tracing (counterpart of fast-wave's CudaTimerSection, fast-wave/src/simulation.cpp:14-33):
  * total number of kernels this library has launched in the process ... */

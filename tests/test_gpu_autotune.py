@@ -17,9 +17,14 @@ def at(monkeypatch, tmp_path):
 
 def test_schedule_lists(rs, cuda):
     lib = rs._lib
-    assert lib.plan_for(4096, 4096, cuda).schedules() == [0, 1, 2, 3, 4, 6, 8, 9, 10, 11, 12, 14]
-    assert lib.plan_for(2048, 2048, cuda).schedules() == [0, 1, 2, 3, 4, 6]  # no split below 4096
-    assert lib.plan_for(8192, 64, cuda).schedules() == [0, 1, 4]
+    # the split-pair family is one schedule where it covers both directions; the compensated
+    # family (bit 16) keeps every single-sequence kernel choice
+    # per direction: the split-pair passes (one schedule), or (bit 16 rows, bit 32 columns) the
+    # single-sequence kernels with their own choices
+    assert lib.plan_for(4096, 4096, cuda).schedules() == [0, 16, 17, 20, 32, 34, 40, 42, 48, 49, 50, 51, 52, 54,
+                                                          56, 57, 58, 59, 60, 62]
+    assert lib.plan_for(2048, 2048, cuda).schedules() == [0, 16, 17, 20, 32, 34, 48, 49, 50, 51, 52, 54]  # no split
+    assert lib.plan_for(8192, 64, cuda).schedules() == [0, 16, 17, 20]  # split-pair rows, 64-point columns
     assert lib.plan_for(72, 40, cuda).schedules() == [0]  # direct-DFT sizes have one schedule
     p = lib.plan_for(1024, 1024, cuda)
     old = p.schedule()
@@ -27,7 +32,7 @@ def test_schedule_lists(rs, cuda):
     assert p.schedule() == 6
     p.set_schedule(old)
     with pytest.raises(Exception):
-        p.set_schedule(16)
+        p.set_schedule(64)
 
 
 @pytest.mark.parametrize("n", [1024, 1536])

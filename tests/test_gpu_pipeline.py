@@ -10,11 +10,14 @@ pytestmark = pytest.mark.gpu
 def run_both(rs, cuda, nx, ny, fn):
     plan = rs._lib.plan_for(nx, ny, cuda)
     outs = []
-    for mask in (0, 1, 2, 3):  # per-block kernels, pipelined rows, pipelined columns, both
-        plan.set_pipeline(mask)
+    old = plan.schedule()
+    # the single-sequence kernels with compensated twiddles (schedule bits 16 | 32): per-block
+    # kernels, pipelined rows, pipelined columns, both
+    for mask in (0, 1, 2, 3):
+        plan.set_schedule(48 | mask)
         outs.append(fn())
         torch.cuda.synchronize()
-    plan.set_pipeline(2)
+    plan.set_schedule(old)
     assert plan.status() == 0
     return outs
 
@@ -64,3 +67,41 @@ def test_multislice_pipeline_bit_identical(rs, cuda, n, pitch):
     for other in runs[1:]:
         for a, b in zip(runs[0], other):
             np.testing.assert_array_equal(a, b)
+
+
+@pytest.mark.parametrize("nx,ny", [(4096, 4096), (1024, 1536), (2048, 2048), (512, 512), (8192, 1024)])
+def test_split_pair_passes_match_compensated_passes(rs, cuda, nx, ny):
+    """The default multislice passes (two rows / two columns per thread group in packed f32x2
+    arithmetic, dithered twiddle tables) against the single-sequence passes with compensated
+    twiddles on the same 12-slice voxel run: equal to FP32 rounding (both are within the FP64
+    accuracy bound; their roundings differ)."""
+    wl = rs.convert_energy_wavelength(25000.0)
+    dx = 0.25e-6
+    pitch = 0.7e-6
+    gx, gy = int(nx * dx / pitch) + 4, int(ny * dx / pitch) + 4
+    rng = np.random.default_rng(nx + 3 * ny)
+    grid = rng.integers(0, 4, size=(12, gy, gx)).astype(np.uint32)
+    s = rs.Sample(z_start=0.5, pixel_size_x=pitch, pixel_size_z=1e-6, grid=grid,
+                  materials=[rs.Material(str(i), 1.0) for i in range(3)], x_positions=np.array([0.1e-6]),
+                  pixel_size_y=pitch, y_positions=np.array([-0.2e-6]))
+    s.db_list = np.array([0, 2e-7 + 1e-10j, 4e-7 + 3e-10j, 1e-7 + 2e-9j])
+    p = rs.SimParams(N=nx * ny, nx=nx, ny=ny, dx=dx, dy=dx, z_detector=1.0, detector_size=nx * dx,
+                     detector_pixel_size_x=dx, detector_pixel_size_y=dx, wl=wl, chunk_size=nx)
+    plan = rs._lib.plan_for(nx, ny, cuda)
+    old = plan.schedule()
+    outs = []
+    try:
+        for mask in (0, 48 | old):
+            plan.set_schedule(mask)
+            x = rng.normal(size=nx * ny) + 1j * rng.normal(size=nx * ny) if not outs else None
+            if x is not None:
+                x0 = x.astype(np.complex64)
+            u, U = rs.GpuVector.from_numpy(x0, cuda), rs.GpuVector.zeros(nx * ny, cuda)
+            s.apply(u, U, p, 0.45 / dx, 0, None)
+            outs.append((u.to_numpy(), U.to_numpy()))
+    finally:
+        plan.set_schedule(old)
+    for a, b in zip(outs[0], outs[1]):
+        assert np.all(np.isfinite(a))
+        assert np.linalg.norm(a - b) / np.linalg.norm(b) < 3e-6
+    assert plan.status() == 0
