@@ -70,6 +70,63 @@ def test_reduce_detector_two_cpu_ranks():
     assert res == {0: 64 * 3.0, 1: 64 * 3.0}
 
 
+def _item_image(it, npx=16):
+    """Host stand-in for one item's detector image: integer counts (so any summation order gives
+    the same float64 sum) placed by the source position and scaled by energy and grid size."""
+    img = torch.zeros((npx, npx), dtype=torch.float64)
+    ix = int(abs(it.x) * 1e6) % npx
+    iy = int(abs(it.y) * 1e6) % npx
+    img[iy, ix] += round(it.energy / 1000.0)
+    img[(iy + 3) % npx, :] += it.n // 512
+    return img
+
+
+def _sharded_rank(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    ms = importlib.import_module("3d_ravesim_gb300.multisim")
+    b = ms.shell_batch(n_sources_side=4, n_energies=5, slices=4, fov=64e-6)
+    seen = []
+
+    def run_items(items):
+        seen.extend(items)
+        out = torch.zeros((16, 16), dtype=torch.float64)
+        for it in items:
+            out += _item_image(it)
+        return out
+    img = ms.run_sharded(b, rank, world, run_items=run_items)
+    q.put((rank, img.numpy().tolist(), [(it.x, it.y, it.energy, it.n) for it in seen]))
+    dist.destroy_process_group()
+
+
+def test_sharded_batch_equals_single_rank_sum():
+    """Two gloo ranks each run their shard of a 80-item batch; after the one reduce every rank
+    holds the single-rank sum of all items bit for bit, and the shards partition the batch."""
+    ms = importlib.import_module("3d_ravesim_gb300.multisim")
+    b = ms.shell_batch(n_sources_side=4, n_energies=5, slices=4, fov=64e-6)
+    whole = torch.zeros((16, 16), dtype=torch.float64)
+    for it in b.items:
+        whole += _item_image(it)
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + (os.getpid() + 7) % 1000
+    procs = [ctx.Process(target=_sharded_rank, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = {}
+    for _ in range(2):
+        rank, img, seen = q.get(timeout=120)
+        res[rank] = (np.array(img), seen)
+    for p in procs:
+        p.join(60)
+    assert all(p.exitcode == 0 for p in procs)
+    for rank in (0, 1):
+        assert np.array_equal(res[rank][0], whole.numpy())
+    keys = sorted(res[0][1] + res[1][1])
+    assert keys == sorted((it.x, it.y, it.energy, it.n) for it in b.items)
+    assert res[0][1] and res[1][1]
+
+
 def test_group_items_by_size_and_energy():
     import importlib
     ms = importlib.import_module("3d_ravesim_gb300.multisim")
