@@ -15,8 +15,37 @@ import torch
 from . import _lib
 
 
+FOUR_STEP_N2 = 256  # the second factor of a four-step axis (n = n1 * 256)
+
+
+def four_step_frequency(n: int) -> np.ndarray:
+    """Frequency index held by each storage entry of a four-step axis of length n: entry i holds
+    frequency i // 256 + (n // 256) * (i % 256)."""
+    i = np.arange(n)
+    return i // FOUR_STEP_N2 + (n // FOUR_STEP_N2) * (i % FOUR_STEP_N2)
+
+
+def natural_from_four_step(flat: np.ndarray, nx: int, ny: int) -> np.ndarray:
+    """A spectrum in four-step storage order (both axes) as the natural-order flat array."""
+    out = np.empty((ny, nx), dtype=flat.dtype)
+    out[np.ix_(four_step_frequency(ny), four_step_frequency(nx))] = np.asarray(flat).reshape(ny, nx)
+    return out.reshape(-1)
+
+
+def four_step_from_natural(flat: np.ndarray, nx: int, ny: int) -> np.ndarray:
+    nat = np.asarray(flat).reshape(ny, nx)
+    return np.ascontiguousarray(nat[np.ix_(four_step_frequency(ny), four_step_frequency(nx))]).reshape(-1)
+
+
 class GpuVector:
-    """A complex64 wave field resident on one CUDA device."""
+    """A complex64 wave field resident on one CUDA device.
+
+    spectrum_order is None when the tensor holds its values in natural order, or
+    ("four_step", nx, ny) when it holds a spectrum that a four-step plan (axes of 32768) left in
+    four-step storage order. Every host read (to_numpy, the chunked callbacks, checkpoints) sees
+    the natural order either way, so U = FFT2(u) holds for callers as in big-wave."""
+
+    spectrum_order = None
 
     def __init__(self, vec: torch.Tensor):
         if not isinstance(vec, torch.Tensor):
@@ -48,7 +77,19 @@ class GpuVector:
         return cls(torch.from_numpy(a).to(device))
 
     def to_numpy(self) -> np.ndarray:
-        return self.vec.detach().cpu().numpy()
+        host = self.vec.detach().cpu().numpy()
+        if self.spectrum_order is not None:
+            _, nx, ny = self.spectrum_order
+            host = natural_from_four_step(host, nx, ny)
+        return host
+
+    def load_natural(self, host: np.ndarray) -> None:
+        """Copy a natural-order host array into the field, in this vector's storage order."""
+        a = np.ascontiguousarray(np.asarray(host, dtype=np.complex64).reshape(-1))
+        if self.spectrum_order is not None:
+            _, nx, ny = self.spectrum_order
+            a = four_step_from_natural(a, nx, ny)
+        self.vec.copy_(torch.from_numpy(a).to(self.device))
 
     @property
     def device(self) -> torch.device:
@@ -93,7 +134,7 @@ class GpuVector:
             chunk = host[i:i + chunk_size]
             fn(i, chunk)
             host[i:i + chunk_size] = chunk
-        self.vec.copy_(torch.from_numpy(host).to(self.device))
+        self.load_natural(host)
 
     def read_chunked(self, chunk_size: int, fn: Callable[[int, np.ndarray], None]) -> None:
         host = self.to_numpy()
@@ -101,16 +142,20 @@ class GpuVector:
             fn(i, host[i:i + chunk_size])
 
     def copy(self) -> "GpuVector":
-        return GpuVector(self.vec.clone())
+        c = GpuVector(self.vec.clone())
+        c.spectrum_order = self.spectrum_order
+        return c
 
     def copy_to(self, destination: "GpuVector") -> None:
         if len(destination) != len(self) or destination.device != self.device:
             destination.vec = self.vec.clone()
         else:
             destination.vec.copy_(self.vec)
+        destination.spectrum_order = self.spectrum_order
 
     def drop(self) -> None:
         self.vec = torch.empty(0, dtype=torch.complex64, device=self.device)
+        self.spectrum_order = None
 
     # -- helpers --------------------------------------------------------------------------
     def _check_2d(self, destination: "GpuVector", nx: int, ny: int) -> None:

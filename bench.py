@@ -40,9 +40,41 @@ UNIT = "slice-steps/s"
 PUBLISHED_MS_PER_LAYER = 43.25
 
 
-# DRAM bytes per launch of the fused passes at 4096^2 from one ncu capture of this workload
-# (profiles/row_pass_col_pipe_4096.md: dram__bytes.sum.per_second x gpu__time_duration.sum)
-NCU_DRAM_BYTES_4096 = {"row_pass": 208.5e6, "col_pass": 215.1e6}
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each fused-pass kernel
+# at 4096^2, from ncu captures of this workload's multislice loop (every launch is a whole-field
+# pass, so a capture of a few slices gives the per-launch figure of the full run). --dram-csv
+# replaces them with the figures of a capture given on the command line.
+NCU_DRAM_BYTES_4096 = {"row_pass_kernel": 208.5e6, "col_pipe_kernel": 215.1e6,
+                       "row_x2_kernel": 208.7e6, "col_x2_pipe_kernel": 215.1e6}
+
+
+def pass_kernels(mask: int, n: int) -> dict:
+    """Kernel that runs the multislice row / column passes of an n x n plan under a schedule mask."""
+    x2_rows = n in (256, 512, 1024, 2048, 4096, 8192)
+    x2_cols = n in (256, 512, 1024, 2048, 4096)
+    rows = "row_x2_kernel" if (x2_rows and not mask & 16) else ("row_pipe_kernel" if mask & 1 else "row_pass_kernel")
+    if x2_cols and not mask & 32:
+        cols = "col_x2_pipe_kernel"
+    else:
+        cols = "col_pipe_kernel" if mask & 2 and not mask & 8 else "col_pass_kernel"
+    return {"row_pass": rows, "col_pass": cols}
+
+
+def dram_bytes_from_csv(path: str) -> dict:
+    """Mean dram__bytes_read.sum + dram__bytes_write.sum per launch, by kernel (template arguments
+    dropped), from an ncu --csv log of those two metrics."""
+    import csv
+    from collections import defaultdict
+    per = defaultdict(lambda: defaultdict(float))
+    with open(path, newline="") as f:
+        rows = [r for r in csv.reader(f) if len(r) > 10]
+    hdr = rows[0]
+    ki, mi, vi, ii = (hdr.index(k) for k in ("Kernel Name", "Metric Name", "Metric Value", "ID"))
+    for r in rows[1:]:
+        if r[mi] in ("dram__bytes_read.sum", "dram__bytes_write.sum"):
+            name = r[ki].split("<")[0].split("(")[0].replace("void ", "").split("::")[-1]
+            per[name][r[ii]] += float(r[vi].replace(",", ""))
+    return {k: sum(v.values()) / len(v) for k, v in per.items()}
 
 
 def parse():
@@ -60,6 +92,9 @@ def parse():
                     help="pass schedule of the field's plan: 'auto' (tuned at start-up) or a mask (1 pipelined "
                          "rows, 2 pipelined columns, 4 general row kernel, 8 split columns)")
     ap.add_argument("--no-extras", action="store_true", help="skip plain/e2e/cpu/accuracy legs")
+    ap.add_argument("--dram-csv", default=None,
+                    help="ncu --csv log of dram__bytes_read.sum and dram__bytes_write.sum for the pass kernels: "
+                         "roofline.traffic from that capture instead of the built-in figures")
     ap.add_argument("--workload", default="talbot", choices=["talbot", "capsule"],
                     help="talbot: the 4096^2 Talbot-Lau benchmark (default); capsule: the 16384^2 "
                          "capsule field (--n 16384 --slices 1024), timed without the extra legs")
@@ -654,12 +689,21 @@ def run_ours(args):
     row_gbs = row_bytes / (row_avg * 1e-3) / 1e9
     col_gbs = col_bytes / (col_avg * 1e-3) / 1e9
     dom = "col_pass" if col_ms.value >= row_ms.value else "row_pass"
+    kernels = pass_kernels(tuned.mask, n)
+    if args.dram_csv:
+        traffic = dram_bytes_from_csv(args.dram_csv)
+        traffic_source = "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, capture given by --dram-csv"
+    else:
+        traffic = NCU_DRAM_BYTES_4096 if n == 4096 else {}
+        traffic_source = ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch of this kernel, one "
+                          "capture of this workload's multislice loop at 4096^2" if n == 4096 else None)
     achieved = col_gbs if dom == "col_pass" else row_gbs
     roofline = {"bound": "hbm", "kernel": f"{dom} (fused {'column FFT*H*IFFT' if dom == 'col_pass' else 'row IFFT*T*FFT'})",
                 "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "peak_kind": peak_kind,
-                "traffic": NCU_DRAM_BYTES_4096[dom] if n == 4096 else None,
-                "traffic_source": "ncu dram bytes per launch, profiles/row_pass_col_pipe_4096.md",
+                "traffic": traffic.get(kernels[dom]),
+                "traffic_source": traffic_source,
+                "kernels": kernels,
                 "row_pass": {"avg_us": round(row_avg * 1e3, 2), "GB_s": round(row_gbs, 1), "launches": nr.value,
                              "algorithmic_bytes": row_bytes},
                 "col_pass": {"avg_us": round(col_avg * 1e3, 2), "GB_s": round(col_gbs, 1), "launches": nc.value,

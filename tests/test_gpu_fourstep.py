@@ -116,6 +116,42 @@ def test_32768_round_trip_and_parseval(rs, cuda):
     torch.cuda.empty_cache()
 
 
+def test_32768_spectrum_reads_as_natural_fft2(rs, cuda):
+    """At 32768^2 U keeps the four-step plan's storage order on the device, but reads as big-wave's
+    U = FFT2(u): bins picked in natural order from U (through the storage index the host reads
+    use) equal a direct DFT of the new u at those bins."""
+    from importlib import import_module
+    vec = import_module("3d_ravesim_gb300.vector")
+    n = 32768
+    p = rs.SimParams(N=n * n, nx=n, ny=n, dx=50e-9, dy=50e-9, z_detector=1.0, detector_size=n * 50e-9,
+                     detector_pixel_size_x=50e-9 * 64, detector_pixel_size_y=50e-9 * 64,
+                     wl=rs.convert_energy_wavelength(30000.0), chunk_size=n)
+    u = rs.GpuVector(field(n, n, 5, cuda))
+    U = rs.GpuVector.zeros(n * n, cuda)
+    rs.propagate_2d(u, U, p.dx, p.dy, p.wl, 2e-4, p.chunk_size, 0.45 / p.dx, n, n)
+    assert U.spectrum_order == ("four_step", n, n)
+    freq = vec.four_step_frequency(n)
+    storage_of = np.empty(n, dtype=np.int64)
+    storage_of[freq] = np.arange(n)
+    rng = np.random.default_rng(11)
+    kx = np.concatenate([[0, 1, n - 1, 5000], rng.integers(0, n, 4)])
+    ky = np.concatenate([[0, n // 2, 2, 7], rng.integers(0, n, 4)])
+    # direct DFT at (ky, kx): X = sum_y e^{-2 pi i ky y/n} sum_x u[y, x] e^{-2 pi i kx x/n}
+    xs = torch.arange(n, device=cuda, dtype=torch.float64)
+    ex = torch.polar(torch.ones(n, len(kx), device=cuda, dtype=torch.float64),
+                     -2 * np.pi * torch.outer(xs, torch.tensor(kx, device=cuda, dtype=torch.float64)) / n)
+    rows = u.vec.view(n, n) @ ex.to(torch.complex64)                       # (n, len(kx))
+    ey = torch.polar(torch.ones(len(ky), n, device=cuda, dtype=torch.float64),
+                     -2 * np.pi * torch.outer(torch.tensor(ky, device=cuda, dtype=torch.float64), xs) / n)
+    direct = (ey @ rows.to(torch.complex128)).diagonal().cpu().numpy()     # X[ky[j], kx[j]]
+    idx = torch.tensor(storage_of[ky] * n + storage_of[kx], device=cuda)
+    got = U.vec[idx].cpu().numpy().astype(np.complex128)
+    scale = np.sqrt(float((u.vec.abs() ** 2).sum().item()) * n * n) / n  # typical |X| of the field
+    assert np.max(np.abs(got - direct)) / scale < 1e-4
+    del u, U, rows, ex, ey
+    torch.cuda.empty_cache()
+
+
 def shell_sample(rs, nz, ny_v, nx_v, pitch, seed=0):
     zz = (np.arange(nz) - (nz - 1) / 2.0)[:, None, None] * pitch
     yy = (np.arange(ny_v) - ny_v / 2.0)[None, :, None] * pitch

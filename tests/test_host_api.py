@@ -75,3 +75,20 @@ def test_multislice_model_rejects_bad_checkpoint_setting():
     for bad in (-1, "sqrt", 2.5):
         with pytest.raises(ValueError):
             adj.MultisliceModel(p, geom, 1e5, torch.ones(64 * 64, dtype=torch.complex64), checkpoint_every=bad)
+
+
+def test_four_step_storage_order_round_trip():
+    """The natural <-> four-step storage reordering of spectra: entry i of an axis holds frequency
+    i // 256 + (n // 256) * (i % 256), and the two conversions invert each other."""
+    import importlib
+    import numpy as np
+    vec = importlib.import_module("3d_ravesim_gb300.vector")
+    nx, ny = 1024, 512
+    f = vec.four_step_frequency(nx)
+    assert sorted(f) == list(range(nx)) and f[1] == nx // 256 and f[256] == 1
+    rng = np.random.default_rng(0)
+    nat = (rng.normal(size=nx * ny) + 1j * rng.normal(size=nx * ny)).astype(np.complex64)
+    st = vec.four_step_from_natural(nat, nx, ny)
+    fy, fx = vec.four_step_frequency(ny), vec.four_step_frequency(nx)
+    assert st.reshape(ny, nx)[3, 7] == nat.reshape(ny, nx)[fy[3], fx[7]]
+    assert np.array_equal(vec.natural_from_four_step(st, nx, ny), nat)
