@@ -68,6 +68,10 @@ _SIGS = {
                               _DP, _DP, c_int, c_int, _P], c_int),
     "rs_multislice_dbgrid_store": ([_P, _P, _P, _P, ctypes.POINTER(VoxelGeom), c_double, c_double, c_double,
                                     c_double, _DP, _DP, c_int, c_int, _P, _P], c_int),
+    "rs_adjoint_multislice_dbgrid_ex": ([_P, _P, _P, ctypes.POINTER(VoxelGeom), c_double, c_double, c_double,
+                                         c_double, _DP, _DP, c_int, c_int, _P, _P, c_uint, _P], c_int),
+    "rs_multislice_dbgrid_fields": ([_P, _P, _P, _P, ctypes.POINTER(VoxelGeom), c_double, c_double, c_double,
+                                     c_double, _DP, _DP, c_int, c_int, _P, _P], c_int),
     "rs_adjoint_multislice_dbgrid": ([_P, _P, _P, ctypes.POINTER(VoxelGeom), c_double, c_double, c_double, c_double,
                                       _DP, _DP, c_int, c_int, _P, _P, _P], c_int),
     "rs_adjoint_slice": ([_P, _P, _P, _P, ctypes.POINTER(VoxelGeom), c_double, c_double, c_double, c_int, c_double,

@@ -45,10 +45,13 @@ class MultisliceModel:
     """Detector image I(delta, beta) of a field u0 through a delta/beta voxel volume."""
 
     def __init__(self, params: SimParams, geom: VolumeGeometry, cutoff: float, u0: torch.Tensor,
-                 checkpoint_every: int | str | None = None, memory_budget_bytes: int | None = None):
+                 checkpoint_every: int | str | None = None, memory_budget_bytes: int | None = None,
+                 keep_tail: int = 2):
         """checkpoint_every: None (about sqrt(nz) slices per segment), a segment length, 0 (keep
         every slice's field), or "auto": keep every field when nz fields fit memory_budget_bytes
-        (default: a quarter of the device's free memory at forward time), else sqrt(nz)."""
+        (default: a quarter of the device's free memory at forward time), else sqrt(nz).
+        keep_tail: with checkpoints, the number of last segments whose fields the forward keeps
+        (the backward starts with them and need not recompute them): 2 * every extra fields."""
         self.p, self.geom, self.cutoff = params, geom, float(cutoff)
         self.u0 = u0
         self.device = u0.device
@@ -57,10 +60,14 @@ class MultisliceModel:
             raise ValueError(f"checkpoint_every must be None, 'auto' or an int >= 0, got {checkpoint_every!r}")
         self.checkpoint_every = checkpoint_every
         self.memory_budget_bytes = memory_budget_bytes
+        if not (isinstance(keep_tail, int) and keep_tail >= 0):
+            raise ValueError(f"keep_tail must be an int >= 0, got {keep_tail!r}")
+        self.keep_tail = keep_tail
         n = params.nx * params.ny
         self.u = GpuVector(torch.empty(n, dtype=torch.complex64, device=self.device))
         self.U = GpuVector(torch.empty(n, dtype=torch.complex64, device=self.device))
         self.checkpoints: dict[int, torch.Tensor] = {}
+        self.tail: dict[int, torch.Tensor] = {}  # first slice -> fields entering a kept segment's slices
         self.u_final = None
         self.last_backward = None  # "fused" (two passes per slice) or "per-slice"
         self.fused = True          # False forces the per-slice backward
@@ -110,9 +117,16 @@ class MultisliceModel:
         else:
             every = mode or max(1, int(round(math.sqrt(nz))))
             self.every = every
-            for s0 in range(0, nz, every):
+            self.tail = {}
+            starts = list(range(0, nz, every))
+            for s0 in starts:
                 self.checkpoints[s0] = self.u.vec.clone()
-                self._step_slices(db, s0, min(nz, s0 + every))
+                s1 = min(nz, s0 + every)
+                # the last keep_tail segments keep their fields as they run: the backward starts
+                # with them and then needs no recomputation of them
+                if s0 in starts[max(0, len(starts) - self.keep_tail):] and self.fused and self._store_segment(db, s0, s1):
+                    continue
+                self._step_slices(db, s0, s1)
         p = self.p
         propagate_2d(self.u, self.U, p.dx, p.get_dy(), p.wl, self._final_dz(nz), p.chunk_size, self.cutoff,
                      p.nx, p.ny, skip_fft=True)
@@ -164,6 +178,24 @@ class MultisliceModel:
         return grad
 
 
+    def _store_segment(self, db: torch.Tensor, s0: int, s1: int) -> bool:
+        """Slices s0..s1-1 keeping the field entering each (self.tail); False if unsupported."""
+        p = self.p
+        plan = _lib.plan_for(p.nx, p.ny, self.device)
+        if not plan.fast or p.nx & (p.nx - 1) or 2 * db.shape[2] > p.nx + p.nx // 16:
+            return False
+        fields = torch.empty((s1 - s0, p.nx * p.ny), dtype=torch.complex64, device=self.device)
+        with torch.cuda.device(self.device):
+            rc = _lib.lib().rs_multislice_dbgrid_store(
+                plan.handle, _lib.ptr(self.u.vec), _lib.ptr(self.U.vec), _lib.ptr(db), self._vgeom(db),
+                float(p.dx), float(p.get_dy()), float(p.wl), self.cutoff, _lib.doubles(self._dz(db.shape[0])), None,
+                s0, s1, _lib.ptr(fields), _lib.stream_handle())
+        if rc == _lib.RS_EUNSUPPORTED:
+            return False
+        _lib.check(rc, "rs_multislice_dbgrid_store")
+        self.tail[s0] = fields
+        return True
+
     def _forward_store_all(self, db: torch.Tensor) -> bool:
         """The whole forward in one fused call that also keeps every slice's entering field;
         False (nothing run) when the size is not supported by the fused adjoint."""
@@ -196,20 +228,31 @@ class MultisliceModel:
                                                             dz, None, 0, nz, _lib.ptr(self.fields), _lib.ptr(grad),
                                                             st), "rs_adjoint_multislice_dbgrid")
             return True
-        fields = torch.empty((self.every, n), dtype=torch.complex64, device=self.device)
-        for s0 in sorted(self.checkpoints, reverse=True):
+        tail = self.tail or {}
+        scratch = None
+        order = sorted(self.checkpoints, reverse=True)
+        for i, s0 in enumerate(order):
             s1 = min(nz, s0 + self.every)
-            self.u.vec.copy_(self.checkpoints[s0])
+            # g stays transformed along x from one segment to the next
+            gflags = (1 if i > 0 else 0) | (2 if i + 1 < len(order) else 0)
             with torch.cuda.device(self.device):
-                rc = lib.rs_multislice_dbgrid_store(plan.handle, _lib.ptr(self.u.vec), _lib.ptr(self.U.vec),
-                                                    _lib.ptr(db), vg, float(p.dx), float(p.get_dy()), float(p.wl),
-                                                    self.cutoff, dz, None, s0, s1, _lib.ptr(fields), st)
-                if rc == _lib.RS_EUNSUPPORTED:
-                    return False
-                _lib.check(rc, "rs_multislice_dbgrid_store")
-                rc = lib.rs_adjoint_multislice_dbgrid(plan.handle, _lib.ptr(g.vec), _lib.ptr(db), vg, float(p.dx),
-                                                      float(p.get_dy()), float(p.wl), self.cutoff, dz, None, s0, s1,
-                                                      _lib.ptr(fields), _lib.ptr(grad), st)
+                fields = tail.get(s0)  # a kept segment's fields are still there
+                if fields is None:
+                    if scratch is None:
+                        scratch = torch.empty((self.every, n), dtype=torch.complex64, device=self.device)
+                    fields = scratch
+                    self.u.vec.copy_(self.checkpoints[s0])
+                    rc = lib.rs_multislice_dbgrid_fields(plan.handle, _lib.ptr(self.u.vec), _lib.ptr(self.U.vec),
+                                                         _lib.ptr(db), vg, float(p.dx), float(p.get_dy()),
+                                                         float(p.wl), self.cutoff, dz, None, s0, s1,
+                                                         _lib.ptr(fields), st)
+                    if rc == _lib.RS_EUNSUPPORTED:
+                        return False
+                    _lib.check(rc, "rs_multislice_dbgrid_fields")
+                rc = lib.rs_adjoint_multislice_dbgrid_ex(plan.handle, _lib.ptr(g.vec), _lib.ptr(db), vg,
+                                                         float(p.dx), float(p.get_dy()), float(p.wl), self.cutoff,
+                                                         dz, None, s0, s1, _lib.ptr(fields), _lib.ptr(grad), gflags,
+                                                         st)
                 if rc == _lib.RS_EUNSUPPORTED:
                     return False
                 _lib.check(rc, "rs_adjoint_multislice_dbgrid")

@@ -140,7 +140,9 @@ struct rs_plan {
   int test_stall = 0;     // one-shot: the next pipelined column pass waits on a barrier nobody completes
   // Split-pair multislice passes (rs_x2.cuh): kDitherTables dithered copies of the row stage table
   // and of the two-level column table, and the matching DFT constants; slice k uses copy k mod K.
-  bool x2r_on = true, x2c_on = true;  // schedule: cleared by RS_SCHED_COMP_ROWS / RS_SCHED_COMP_COLS
+  // schedule: cleared by RS_SCHED_COMP_ROWS / RS_SCHED_COMP_COLS; the default runs the split-pair
+  // column passes and the single-sequence rows (measured faster rows at 2048^2 and 4096^2)
+  bool x2r_on = false, x2c_on = true;
   bool x2_rows = false, x2_cols = false;  // available for this plan's sizes
   void* twd_arena = nullptr;
   float4* twd_x = nullptr;
@@ -516,6 +518,7 @@ struct SliceSource {
   int f64 = 1;
   PlasmaArgs pl_base{};
   float2* store = nullptr;     // optional: the field entering slice z goes to store + (z - s0) * nx * ny
+  bool fields_only = false;    // with store: stop once the last field is stored (u, U left unspecified)
 };
 
 // Shared driver of the voxel and plasma multislice entry points.
@@ -544,8 +547,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
   // slice z's forward transform and slice z + 1's inverse use dithered table z mod K, so every
   // transform is undone by one with the same table.
   const bool plasma_rows_vox = !src.plasma || (p->fast && p->row_vox && !src.store);
-  const bool x2r = p->fast && p->x2r_on && p->x2_rows && !src.store && plasma_rows_vox &&
-                   g->nx_v <= row_x2_slots(p->nx);
+  const bool x2r = p->fast && p->x2r_on && p->x2_rows && plasma_rows_vox && g->nx_v <= row_x2_slots(p->nx);
   auto table_x = [&](int z) { return p->twd_x + static_cast<size_t>(z % kDitherTables) * p->twd_x_len; };
   double cur_dz = NAN, cur_cs = NAN;
   for (int z = s0; z < s1; ++z) {
@@ -599,7 +601,9 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       RowArgs r{};
       r.in = u; r.out = u; r.ny = p->ny * src.batch; r.tw = p->tws_x; r.ax = axis_tab(p);
       r.axis_rows = src.batch > 1 ? p->ny : 0;
-      r.flags = (z == s0 ? 0 : ROW_INV) | ROW_FWD | (src.plasma && !plasma_plane ? ROW_TPLASMA : ROW_TVOX);
+      const bool last_field = src.fields_only && z == s1 - 1;  // nothing after its store is needed
+      r.flags = (z == s0 ? 0 : ROW_INV) |
+                (last_field ? 0 : ROW_FWD | (src.plasma && !plasma_plane ? ROW_TPLASMA : ROW_TVOX));
       if (src.store) {
         r.flags |= ROW_STORE_U;
         r.aux = src.store + static_cast<size_t>(z - s0) * p->nx * p->ny;
@@ -619,6 +623,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
         RS_CK(run_row(p, r, s));
       }
       prof_end(p, er, s);
+      if (last_field) break;
       ColArgs c{};
       c.in = u; c.out = u; c.spec = U; c.nx = p->nx; c.tw = p->tws_y;
       c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
@@ -635,7 +640,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       RS_TRY(generic_slice(p, u, U, src.plasma ? nullptr : &vox, src.plasma ? &pl : nullptr, s));
     }
   }
-  if (p->fast) {
+  if (p->fast && !src.fields_only) {
     RowArgs r{};
     r.in = u; r.out = u; r.ny = p->ny * src.batch; r.tw = p->tws_x; r.flags = ROW_INV;
     if (x2r) {
@@ -1394,12 +1399,38 @@ int rs_multislice_dbgrid_store(rs_plan* p, void* u, void* U, const float* db_gri
                     slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
 }
 
+int rs_multislice_dbgrid_fields(rs_plan* p, void* u, void* U, const float* db_grid, const rs_voxel_geom* geom,
+                                double dx, double dy, double wl, double cutoff, const double* slice_dz,
+                                const double* coord_scale, int slice_begin, int slice_end, void* fields,
+                                void* stream) {
+  StatusNote sn_(p, stream);
+  RS_TRY(check_plan_std(p, "rs_multislice_dbgrid_fields"));
+  if (!db_grid || !fields) return fail(RS_EINVAL, "db_grid and fields must be device pointers");
+  if (!p->fast) return fail(RS_EUNSUPPORTED, "field storing needs the fused passes (fast sizes)");
+  SliceSource src;
+  src.dbv = reinterpret_cast<const float2*>(db_grid);
+  src.n_db = 1;
+  src.store = static_cast<float2*>(fields);
+  src.fields_only = true;
+  return multislice(p, static_cast<float2*>(u), static_cast<float2*>(U), src, geom, dx, dy, wl, cutoff,
+                    slice_dz, coord_scale, slice_begin, slice_end, as_stream(stream));
+}
+
 int rs_adjoint_multislice_dbgrid(rs_plan* p, void* g, const float* db_grid, const rs_voxel_geom* geom, double dx,
                                  double dy, double wl, double cutoff, const double* slice_dz,
                                  const double* coord_scale, int slice_begin, int slice_end, const void* fields,
                                  float* grad_grid, void* stream) {
+  return rs_adjoint_multislice_dbgrid_ex(p, g, db_grid, geom, dx, dy, wl, cutoff, slice_dz, coord_scale, slice_begin,
+                                         slice_end, fields, grad_grid, 0u, stream);
+}
+
+int rs_adjoint_multislice_dbgrid_ex(rs_plan* p, void* g, const float* db_grid, const rs_voxel_geom* geom, double dx,
+                                    double dy, double wl, double cutoff, const double* slice_dz,
+                                    const double* coord_scale, int slice_begin, int slice_end, const void* fields,
+                                    float* grad_grid, unsigned gflags, void* stream) {
   StatusNote sn_(p, stream);
   RS_TRY(check_plan_std(p, "rs_adjoint_multislice_dbgrid"));
+  if (gflags & ~(RS_ADJ_G_XSPEC_IN | RS_ADJ_G_XSPEC_OUT)) return fail(RS_EINVAL, "unknown flags 0x%x", gflags);
   if (!g || !db_grid || !fields || !grad_grid || !geom || !slice_dz) return fail(RS_EINVAL, "NULL pointer argument");
   if (geom->nz <= 0 || geom->ny_v < 2 || geom->nx_v < 2) return fail(RS_EINVAL, "bad grid shape");
   if (slice_begin < 0 || slice_end > geom->nz || slice_begin > slice_end)
@@ -1428,7 +1459,7 @@ int rs_adjoint_multislice_dbgrid(rs_plan* p, void* g, const float* db_grid, cons
       RS_TRY(build_axes(p, geom, dx, dy, cs, s));
       cur_cs = cs;
     }
-    if (z == slice_end - 1) {
+    if (z == slice_end - 1 && !(gflags & RS_ADJ_G_XSPEC_IN)) {
       RowArgs r{};
       r.in = gv; r.out = gv; r.ny = p->ny; r.tw = p->tws_x; r.flags = ROW_FWD;
       RS_CK(run_row(p, r, s));
@@ -1437,10 +1468,11 @@ int rs_adjoint_multislice_dbgrid(rs_plan* p, void* g, const float* db_grid, cons
     c.in = gv; c.out = gv; c.spec = nullptr; c.nx = p->nx; c.tw = p->tws_y;
     c.ex = p->ex; c.ey = p->ey; c.ylim = p->ylim; c.scale = inv_n;
     c.flags = COL_FWD | COL_H | COL_SCALE | COL_INV;
-    RS_CK(run_col(p, c, s));
+    bool col_x2 = false;
+    RS_CK(run_col_ms(p, c, z % kDitherTables, &col_x2, s));
     RowArgs r{};
     r.in = gv; r.out = gv; r.ny = p->ny; r.tw = p->tws_x; r.ax = axis_tab(p);
-    r.flags = ROW_INV | (z > slice_begin ? ROW_FWD : 0);
+    r.flags = ROW_INV | (z > slice_begin || (gflags & RS_ADJ_G_XSPEC_OUT) ? ROW_FWD : 0);
     r.vox.dbv = reinterpret_cast<const float2*>(db_grid) + plane * z;
     r.vox.nxv = geom->nx_v;
     r.vox.nyv = geom->ny_v;

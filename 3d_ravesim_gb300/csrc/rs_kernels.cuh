@@ -541,9 +541,13 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
 // [row IFFT] -> v = P^H g' in the spatial domain; with u the field that entered the slice (aux)
 // and t its transmission, accumulate dL/ddelta = 4 pi a Im(t conj(G)), dL/dbeta =
 // -4 pi a Re(t conj(G)), G = conj(u) v, through the bilinear weights into `grad`, and continue
-// with conj(t) v -> [row FFT]. The y-blended (delta, beta) row and the two voxel rows' gradient
-// sums live in the exchange buffer (3 nxv float pairs; the host checks nxv <= S/3), and each
-// block adds its sums to the grid with one global atomic per touched value.
+// with conj(t) v -> [row FFT]. The y-blended (delta, beta) row and the x-weighted gradient sums
+// live in the exchange buffer (the host checks nxv <= S/2). Consecutive lanes hold consecutive
+// pixels, several of which fall in one voxel column, so the sums are kept in up to four copies
+// (lane mod copies) to spread the shared-memory atomics over distinct addresses; the copies are
+// added up per voxel, and each block adds its sums to the grid with one global atomic per touched
+// value. The y weights (1 - fy, fy) are the same for every pixel of the row, so they are applied
+// once per voxel.
 template <int N, int ROWS>
 __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row_adjoint_kernel(const RowArgs a) {
   using P = FftPlan<N>;
@@ -576,17 +580,18 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = valid ? a.in[rbase + slot_pos<N, RF>(t, e)] : make_float2(0.f, 0.f);
   }
-  // x-weighted gradient sums of the row, [nxv][delta, beta]; the y weights (1 - fy, fy) are the
-  // same for every pixel of the row, so they are applied once per voxel when the sums are added
-  // to the two voxel rows
+  // copies of the sums: [copy][nxv + 1][delta, beta] after the nxv staged (delta, beta) values
+  const int stride = 2 * (nxv + 1);
+  const int copies = max(1, min(4, (P::S - nxv) / (nxv + 1)));  // one copy always fits (nxv <= S/2)
   float* acc = reinterpret_cast<float*>(buf + nxv);
   if (yi >= 0) {
     for (int j = t; j < nxv; j += T) buf[j] = voxel_col_blend(a.vox, j, yi, fy);
-    for (int j = t; j < 2 * nxv; j += T) acc[j] = 0.0f;
+    for (int j = t; j < copies * stride; j += T) acc[j] = 0.0f;
   }
   __syncthreads();
   if (yi >= 0) {
     const float k = 12.566370614359172f * a.vox.a;  // 4 pi t / wl
+    float* mine = acc + (threadIdx.x % copies) * stride;
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       const int x = slot_pos<N, RF>(t, e);
@@ -601,7 +606,7 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
       const float2 q = cmulc(tr, G);      // t conj(G)
       const float gd = k * q.y, gb = -k * q.x;
       const float gx0 = 1.0f - fx;
-      float* r0 = acc + 2 * xi;
+      float* r0 = mine + 2 * xi;
       atomicAdd(r0, gx0 * gd);
       atomicAdd(r0 + 1, gx0 * gb);
       atomicAdd(r0 + 2, fx * gd);
@@ -614,7 +619,8 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
     float* g0 = a.grad + static_cast<size_t>(yi) * nxv * 2;  // rows yi and yi + 1 are contiguous
     const float gy0 = 1.0f - fy;
     for (int j = t; j < 2 * nxv; j += T) {
-      const float val = acc[j];
+      float val = acc[j];
+      for (int c = 1; c < copies; ++c) val += acc[c * stride + j];
       if (val != 0.0f) {
         atomicAdd(&g0[j], gy0 * val);
         if (fy != 0.0f) atomicAdd(&g0[2 * nxv + j], fy * val);

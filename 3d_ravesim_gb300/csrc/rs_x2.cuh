@@ -85,8 +85,9 @@ __device__ __forceinline__ float2 x2_col_blend(const VoxelArgs& v, const uint32_
   return voxel_col_blend(v, j, yi, fy);
 }
 
-// Flags: ROW_INV (inverse transform first, with twd_inv), ROW_TVOX (voxel transmission),
-// ROW_FWD (forward transform last, with twd_fwd), ROW_SCALE. Rows 2p and 2p + 1 form pair p.
+// Flags: ROW_INV (inverse transform first, with twd_inv), ROW_STORE_U (the spatial rows entering
+// the transmission to aux), ROW_TVOX (voxel transmission), ROW_FWD (forward transform last, with
+// twd_fwd), ROW_SCALE. Rows 2p and 2p + 1 form pair p.
 template <int N>
 __global__ void __launch_bounds__(RowX2Geom<N>::THREADS, RowX2Geom<N>::MINB) row_x2_kernel(const RowArgs a) {
   using P = FftPlan<N>;
@@ -151,6 +152,16 @@ __global__ void __launch_bounds__(RowX2Geom<N>::THREADS, RowX2Geom<N>::MINB) row
     v[e] = cp2{make_float2(fa.x, fb.x), make_float2(fa.y, fb.y)};
   }
   if (inv) fft_seq2x<N, true>(v, buf, t, a.twd_inv, dft_k(a.k_inv));
+  if (flags & ROW_STORE_U) {  // the spatial rows entering the transmission (for the adjoint sweep)
+    float2* auxA = a.aux + static_cast<size_t>(validA ? rowA : 0) * N;
+    float2* auxB = a.aux + static_cast<size_t>(validB ? rowB : 0) * N;
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      const int pos = slot_pos<N, RF>(t, e);
+      if (validA) auxA[pos] = make_float2(v[e].re.x, v[e].im.x);
+      if (validB) auxB[pos] = make_float2(v[e].re.y, v[e].im.y);
+    }
+  }
 
   if (tvox) {
     // The exchange buffer is idle between the transforms: stage the y-blended voxel rows of both

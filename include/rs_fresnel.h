@@ -187,6 +187,15 @@ int rs_multislice_dbgrid_store(rs_plan* plan, void* u, void* U, const float* db_
                                const double* coord_scale, int slice_begin, int slice_end, void* fields,
                                void* stream);
 
+/* The fields of rs_multislice_dbgrid_store alone: the same slices and the same field written for
+ * each, but the work after the last field's store (its transmission, its Fresnel step and the
+ * return of u to real space) is skipped, so u and U are left unspecified. The recomputation step
+ * of a checkpointed adjoint, which only reads the fields. No counterpart in the reference. */
+int rs_multislice_dbgrid_fields(rs_plan* plan, void* u, void* U, const float* db_grid, const rs_voxel_geom* geom,
+                                double dx, double dy, double wl, double cutoff, const double* slice_dz,
+                                const double* coord_scale, int slice_begin, int slice_end, void* fields,
+                                void* stream);
+
 /* Backward sweep of rs_multislice_dbgrid over slices [slice_begin, slice_end) in two fused passes
  * per slice. On entry g = dL/dconj(u_end), the gradient with respect to the field leaving
  * slice_end - 1; on exit g = dL/dconj(u_begin). fields holds the fields entering each slice as
@@ -198,6 +207,17 @@ int rs_adjoint_multislice_dbgrid(rs_plan* plan, void* g, const float* db_grid, c
                                  double dy, double wl, double cutoff, const double* slice_dz,
                                  const double* coord_scale, int slice_begin, int slice_end, const void* fields,
                                  float* grad_grid, void* stream);
+/* The same sweep with g kept transformed along x between segments of a checkpointed backward:
+ * RS_ADJ_G_XSPEC_IN, g arrives as row spectra (the previous segment's output, not real space);
+ * RS_ADJ_G_XSPEC_OUT, g is left as row spectra for the next segment instead of being returned to
+ * real space. A backward over segments passes OUT on every segment but the last and IN on every
+ * segment but the first, which saves one row transform pair per segment boundary. */
+#define RS_ADJ_G_XSPEC_IN 1u
+#define RS_ADJ_G_XSPEC_OUT 2u
+int rs_adjoint_multislice_dbgrid_ex(rs_plan* plan, void* g, const float* db_grid, const rs_voxel_geom* geom,
+                                    double dx, double dy, double wl, double cutoff, const double* slice_dz,
+                                    const double* coord_scale, int slice_begin, int slice_end, const void* fields,
+                                    float* grad_grid, unsigned flags, void* stream);
 
 /* Adjoint of one slice u' = P (t * u) of rs_multislice_dbgrid. On entry v holds P^H g' (g' =
  * dL/dconj(u'), P^H = a Fresnel step of -dz with the same cutoff); u is the field that entered

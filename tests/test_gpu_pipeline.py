@@ -105,3 +105,40 @@ def test_split_pair_passes_match_compensated_passes(rs, cuda, nx, ny):
         assert np.all(np.isfinite(a))
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 3e-6
     assert plan.status() == 0
+
+
+@pytest.mark.parametrize("n", [1024, 2048])
+def test_split_pair_rows_store_the_entering_fields(rs, cuda, n):
+    """rs_multislice_dbgrid_store and rs_multislice_dbgrid_fields with the split-pair row passes
+    (schedule 0) write the same fields, to FP32 rounding, as the single-sequence kernels (48), and
+    the fields-only form writes exactly what the storing forward writes."""
+    lib = rs._lib
+    rng = np.random.default_rng(n)
+    nz, nv = 6, n // 4 + 4
+    db = torch.from_numpy(np.stack([rng.uniform(0, 3e-7, (nz, nv, nv)), rng.uniform(0, 1e-9, (nz, nv, nv))], -1)
+                          .astype(np.float32)).to(cuda)
+    dx = 0.5e-6
+    geom = lib.VoxelGeom(nz, nv, nv, 4 * dx, 4 * dx, 2e-6, 0.0, 0.0)
+    dz = lib.doubles([2e-6] * nz)
+    plan = lib.plan_for(n, n, cuda)
+    old = plan.schedule()
+    u0 = torch.polar(torch.ones(n * n), torch.from_numpy(rng.uniform(0, 6, n * n)).float()).to(torch.complex64).to(cuda)
+    out = {}
+    try:
+        for mask in (0, 48):
+            plan.set_schedule(mask)
+            for name in ("rs_multislice_dbgrid_store", "rs_multislice_dbgrid_fields"):
+                u, U = u0.clone(), torch.empty_like(u0)
+                fields = torch.zeros((nz, n * n), dtype=torch.complex64, device=cuda)
+                lib.check(getattr(lib.lib(), name)(plan.handle, lib.ptr(u), lib.ptr(U), lib.ptr(db), geom, dx, dx,
+                                                   6.2e-11, 0.45 / dx, dz, None, 0, nz, lib.ptr(fields),
+                                                   lib.stream_handle()), name)
+                torch.cuda.synchronize()
+                out[(mask, name)] = fields.cpu().numpy()
+    finally:
+        plan.set_schedule(old)
+    for mask in (0, 48):
+        assert np.array_equal(out[(mask, "rs_multislice_dbgrid_store")], out[(mask, "rs_multislice_dbgrid_fields")])
+    a, b = out[(0, "rs_multislice_dbgrid_store")], out[(48, "rs_multislice_dbgrid_store")]
+    assert np.array_equal(a[0], b[0])  # the field entering the first slice is the input
+    assert np.linalg.norm(a - b) / np.linalg.norm(b) < 3e-6
