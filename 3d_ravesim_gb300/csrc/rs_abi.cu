@@ -151,7 +151,7 @@ struct rs_plan {
   DftConsts kconst[kDitherTables];
   struct MapEntry {
     const void* ptr = nullptr;
-    int w = 0, bh = 0;
+    int w = 0, bh = 0, depth = 1;
     CUtensorMap map;
   };
   MapEntry maps[4];
@@ -264,17 +264,20 @@ bool tensor_map_encoder() {
 
 bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
-// Tensor map of a (ny, nx) complex64 field viewed as 8-byte elements, box (w columns, bh rows).
-const CUtensorMap* field_map(rs_plan* p, const void* base, int w, int bh) {
+// Tensor map of a stack of `depth` (ny, nx) complex64 fields viewed as 8-byte elements (3D: x, y,
+// field), box (w columns, bh rows, one field); depth 1 for a single field.
+const CUtensorMap* field_map(rs_plan* p, const void* base, int w, int bh, int depth = 1) {
   for (auto& m : p->maps)
-    if (m.ptr == base && m.w == w && m.bh == bh) return &m.map;
+    if (m.ptr == base && m.w == w && m.bh == bh && m.depth == depth) return &m.map;
   auto& slot = p->maps[p->map_next];
   p->map_next = (p->map_next + 1) % 4;
-  cuuint64_t dims[2] = {static_cast<cuuint64_t>(p->nx), static_cast<cuuint64_t>(p->ny)};
-  cuuint64_t strides[1] = {static_cast<cuuint64_t>(p->nx) * 8};
-  cuuint32_t box[2] = {static_cast<cuuint32_t>(w), static_cast<cuuint32_t>(bh)};
-  cuuint32_t es[2] = {1, 1};
-  const CUresult r = g_encode(&slot.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<void*>(base), dims, strides,
+  cuuint64_t dims[3] = {static_cast<cuuint64_t>(p->nx), static_cast<cuuint64_t>(p->ny),
+                        static_cast<cuuint64_t>(depth)};
+  cuuint64_t strides[2] = {static_cast<cuuint64_t>(p->nx) * 8,
+                           static_cast<cuuint64_t>(p->nx) * static_cast<cuuint64_t>(p->ny) * 8};
+  cuuint32_t box[3] = {static_cast<cuuint32_t>(w), static_cast<cuuint32_t>(bh), 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  const CUresult r = g_encode(&slot.map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<void*>(base), dims, strides,
                               box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) {
@@ -284,6 +287,7 @@ const CUtensorMap* field_map(rs_plan* p, const void* base, int w, int bh) {
   slot.ptr = base;
   slot.w = w;
   slot.bh = bh;
+  slot.depth = depth;
   return &slot.map;
 }
 
@@ -319,20 +323,23 @@ cudaError_t run_col_split(rs_plan* p, const ColArgs& c, cudaStream_t s) {
 }
 
 cudaError_t run_col(rs_plan* p, const ColArgs& ca, cudaStream_t s) {
-  const bool stacked = ca.batches > 1;  // stacked fields: the per-block kernel's batches
+  const bool stacked = ca.batches > 1;  // stacked fields: a batch of equal fields, bstride apart
   if (!stacked && p->split_cols && p->split_ok && ca.flags == (COL_FWD | COL_H | COL_SCALE | COL_INV) &&
       ca.ey == p->ey)
     return run_col_split(p, ca, s);
   ColArgs c = ca;
   c.tw2 = p->tw2_y;
   int w = 0, bh = 0;
-  if (!stacked && p->pipe_cols && col_pipe_box(p->ny, &w, &bh) && aligned16(c.in) && aligned16(c.out) &&
-      tensor_map_encoder()) {
+  const int depth = stacked ? ca.batches : 1;
+  // the pipeline takes a stack whose fields follow each other without gaps (3D tensor maps)
+  const bool dense = !stacked || ca.bstride == static_cast<long long>(p->nx) * p->ny;
+  if (dense && c.pitch == 0 && c.tw4 == 0 && !c.kyi && p->pipe_cols && col_pipe_box(p->ny, &w, &bh) &&
+      aligned16(c.in) && aligned16(c.out) && tensor_map_encoder()) {
     // Copy the input map before the output lookup: encoding the output may recycle its slot.
-    const CUtensorMap* mi = field_map(p, c.in, w, bh);
+    const CUtensorMap* mi = field_map(p, c.in, w, bh, depth);
     if (mi) {
       const CUtensorMap in_copy = *mi;
-      const CUtensorMap* mo = field_map(p, c.out, w, bh);
+      const CUtensorMap* mo = field_map(p, c.out, w, bh, depth);
       if (mo) {
         p->status_pending = true;
         c.test_stall = p->test_stall;
@@ -350,12 +357,14 @@ cudaError_t run_col(rs_plan* p, const ColArgs& ca, cudaStream_t s) {
 cudaError_t run_col_ms(rs_plan* p, const ColArgs& ca, int j, bool* used, cudaStream_t s) {
   *used = false;
   int w = 0, bh = 0;
-  if (p->x2c_on && p->x2_cols && ca.batches <= 1 && col_x2_box(p->ny, &w, &bh) && aligned16(ca.in) &&
-      aligned16(ca.out) && tensor_map_encoder()) {
-    const CUtensorMap* mi = field_map(p, ca.in, w, bh);
+  const int depth = ca.batches > 1 ? ca.batches : 1;
+  const bool dense = depth == 1 || ca.bstride == static_cast<long long>(p->nx) * p->ny;
+  if (p->x2c_on && p->x2_cols && dense && ca.pitch == 0 && ca.tw4 == 0 && !ca.kyi && col_x2_box(p->ny, &w, &bh) &&
+      aligned16(ca.in) && aligned16(ca.out) && tensor_map_encoder()) {
+    const CUtensorMap* mi = field_map(p, ca.in, w, bh, depth);
     if (mi) {
       const CUtensorMap in_copy = *mi;
-      const CUtensorMap* mo = field_map(p, ca.out, w, bh);
+      const CUtensorMap* mo = field_map(p, ca.out, w, bh, depth);
       if (mo) {
         ColArgs c = ca;
         c.twd = p->twd_y2 + static_cast<size_t>(j) * p->twd_y2_len;

@@ -49,7 +49,7 @@ cudaError_t launch_col_x2_n(const ColArgs& a, const CUtensorMap& in, const CUten
     grid_cache[dev & 31] = resident_grid(col_x2_pipe_kernel<N>, G::THREADS, G::SMEM, 1 << 30);
     configured |= bit;
   }
-  const int tiles = (a.nx + G::W - 1) / G::W;
+  const int tiles = (a.nx + G::W - 1) / G::W * (a.batches > 1 ? a.batches : 1);
   const int grid = tiles < grid_cache[dev & 31] ? tiles : grid_cache[dev & 31];
   col_x2_pipe_kernel<N><<<grid, G::THREADS, G::SMEM, s>>>(a, in, out, status);
   const cudaError_t e = cudaGetLastError();

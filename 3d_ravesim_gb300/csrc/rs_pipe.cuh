@@ -75,6 +75,20 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
                "r"(x), "r"(y), "r"(smem_addr(src))
                : "memory");
 }
+// 3D forms: field z of a stack of equal fields (the tensor map's third dimension)
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(
+          smem_addr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_addr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_store_3d(const CUtensorMap* map, int x, int y, int z, const void* src) {
+  asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                   reinterpret_cast<uint64_t>(map)),
+               "r"(x), "r"(y), "r"(z), "r"(smem_addr(src))
+               : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 template <int K>
 __device__ __forceinline__ void bulk_wait_read() {
@@ -313,7 +327,10 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
   const int c = threadIdx.x % W;
   const int t = threadIdx.x / W;
   const int nx = a.nx;
-  const int ntiles = (nx + W - 1) / W;
+  // tiles run over the strips of every field of a stack (the maps are 3D: x, y, field)
+  const int strips = (nx + W - 1) / W;
+  const int nfields = a.batches > 1 ? a.batches : 1;
+  const int ntiles = strips * nfields;
   const int flags = a.flags;
   if (threadIdx.x == 0) {
     for (int b = 0; b < G::NB; ++b) mbar_init(&bars[b], 1);
@@ -348,7 +365,8 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
   int tile = blockIdx.x;
   if (threadIdx.x == 0 && tile < ntiles) {
     mbar_arrive_expect(&bars[0], TILE_BYTES);
-    for (int k = 0; k < N / G::BH; ++k) tma_load_2d(tiles + k * G::BH * W, &map_in, tile * W, k * G::BH, &bars[0]);
+    for (int k = 0; k < N / G::BH; ++k)
+      tma_load_3d(tiles + k * G::BH * W, &map_in, (tile % strips) * W, k * G::BH, tile / strips, &bars[0]);
   }
   bool ok = true;
   for (int i = 0; tile < ntiles && ok; ++i, tile += gridDim.x) {
@@ -364,12 +382,14 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
         const int bn = (i + 1) % G::NB;
         mbar_arrive_expect(&bars[bn], TILE_BYTES);
         for (int k = 0; k < N / G::BH; ++k)
-          tma_load_2d(tiles + bn * G::TILE + k * G::BH * W, &map_in, next * W, k * G::BH, &bars[bn]);
+          tma_load_3d(tiles + bn * G::TILE + k * G::BH * W, &map_in, (next % strips) * W, k * G::BH,
+                      next / strips, &bars[bn]);
       }
     };
     ok = __syncthreads_and(mbar_wait_bounded(&bars[b], (i / G::NB) & 1, status));
     if (!ok) break;
-    const int x = tile * W + c;
+    const int fb = tile / strips;  // field of the stack
+    const int x = (tile % strips) * W + c;
     const bool live = x < nx;
     float2* col = tb + c;
     float2 v[E];
@@ -407,7 +427,8 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
     prefetch_next();
     if ((flags & COL_SPEC) && live) {
 #pragma unroll
-      for (int e = 0; e < E; ++e) a.spec[static_cast<size_t>(col_exit_pos<N, G::L2>(t, e)) * nx + x] = v[e];
+      for (int e = 0; e < E; ++e)
+        a.spec[static_cast<size_t>(fb) * a.bstride + static_cast<size_t>(col_exit_pos<N, G::L2>(t, e)) * nx + x] = v[e];
     }
     if ((flags & COL_SCALE) && !fold) {
 #pragma unroll
@@ -427,7 +448,8 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
-      for (int k = 0; k < N / G::BH; ++k) tma_store_2d(&map_out, tile * W, k * G::BH, tb + k * G::BH * W);
+      for (int k = 0; k < N / G::BH; ++k)
+        tma_store_3d(&map_out, (tile % strips) * W, k * G::BH, fb, tb + k * G::BH * W);
       bulk_commit();
     }
   }

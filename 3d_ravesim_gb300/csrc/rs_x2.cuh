@@ -267,7 +267,9 @@ __global__ void __launch_bounds__(ColX2Geom<N>::THREADS, 1)
   const int p = threadIdx.x % PAIRS;  // pair within the strip
   const int t = threadIdx.x / PAIRS;
   const int nx = a.nx;
-  const int ntiles = (nx + W - 1) / W;
+  // tiles run over the strips of every field of a stack (the maps are 3D: x, y, field)
+  const int strips = (nx + W - 1) / W;
+  const int ntiles = strips * (a.batches > 1 ? a.batches : 1);
   const int flags = a.flags;
   if (threadIdx.x == 0) {
     for (int b = 0; b < G::NB; ++b) mbar_init(&bars[b], 1);
@@ -281,7 +283,8 @@ __global__ void __launch_bounds__(ColX2Geom<N>::THREADS, 1)
   int tile = blockIdx.x;
   if (threadIdx.x == 0 && tile < ntiles) {  // the first strip, before the tables are staged
     mbar_arrive_expect(&bars[0], TILE_BYTES);
-    for (int kb = 0; kb < N / G::BH; ++kb) tma_load_2d(tiles + kb * G::BH * W, &map_in, tile * W, kb * G::BH, &bars[0]);
+    for (int kb = 0; kb < N / G::BH; ++kb)
+      tma_load_3d(tiles + kb * G::BH * W, &map_in, (tile % strips) * W, kb * G::BH, tile / strips, &bars[0]);
   }
   if constexpr (G::TW_SMEM) {
     for (int i = threadIdx.x; i < G::TW_LEN; i += blockDim.x) tw_s[i] = __ldg(&a.twd[i]);
@@ -310,10 +313,12 @@ __global__ void __launch_bounds__(ColX2Geom<N>::THREADS, 1)
         const int bn = (i + 1) % G::NB;
         mbar_arrive_expect(&bars[bn], TILE_BYTES);
         for (int kb = 0; kb < N / G::BH; ++kb)
-          tma_load_2d(tiles + bn * G::TILE + kb * G::BH * W, &map_in, next * W, kb * G::BH, &bars[bn]);
+          tma_load_3d(tiles + bn * G::TILE + kb * G::BH * W, &map_in, (next % strips) * W, kb * G::BH,
+                      next / strips, &bars[bn]);
       }
     };
-    const int xA = tile * W + 2 * p;
+    const int fb = tile / strips;  // field of the stack
+    const int xA = (tile % strips) * W + 2 * p;
     const int xB = xA + 1;
     const bool liveA = xA < nx, liveB = xB < nx;
     // the strip's per-column tables, fetched while its copy lands
@@ -355,7 +360,7 @@ __global__ void __launch_bounds__(ColX2Geom<N>::THREADS, 1)
     if (flags & COL_SPEC) {
 #pragma unroll
       for (int e = 0; e < 16; ++e) {
-        const size_t r = static_cast<size_t>(col_exit_pos<N, true>(t, e)) * nx;
+        const size_t r = static_cast<size_t>(fb) * a.bstride + static_cast<size_t>(col_exit_pos<N, true>(t, e)) * nx;
         if (liveA) a.spec[r + xA] = make_float2(v[e].re.x, v[e].im.x);
         if (liveB) a.spec[r + xB] = make_float2(v[e].re.y, v[e].im.y);
       }
@@ -373,7 +378,8 @@ __global__ void __launch_bounds__(ColX2Geom<N>::THREADS, 1)
     fence_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
-      for (int kb = 0; kb < N / G::BH; ++kb) tma_store_2d(&map_out, tile * W, kb * G::BH, tb + kb * G::BH * W);
+      for (int kb = 0; kb < N / G::BH; ++kb)
+        tma_store_3d(&map_out, (tile % strips) * W, kb * G::BH, fb, tb + kb * G::BH * W);
       bulk_commit();
     }
   }

@@ -521,14 +521,18 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
     graphed.replay()
     out["fused_graph_s"] = round(time.perf_counter() - t0, 3)
     del graphed
-    # the full batch (1024 items) through the fused runner and the plain loop
+    # the full batch (1024 items) through the fused runner (per item, and with the items of one
+    # size and energy stacked into one field stack per launch) and the plain loop
     full = ms.shell_batch()
     per_item = ms.BatchRunner(full, device, streams=2)
     per_item.run(full.items[:4])
+    stacked = ms.BatchRunner(full, device, streams=2)
+    stacked.run(full.items[:40], stacked=True)
     plain_full = ms.BatchRunner(full, device, streams=1)
     plain_full.run(full.items[:1], plain=True)
     full_out = {}
-    for name, runner, kw in (("fused", per_item, {}), ("plain_loop", plain_full, {"plain": True})):
+    for name, runner, kw in (("fused", per_item, {}), ("fused_stacked", stacked, {"stacked": True}),
+                             ("plain_loop", plain_full, {"plain": True})):
         runner.zero()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -536,7 +540,7 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
         torch.cuda.synchronize()
         full_out[name + "_s"] = round(time.perf_counter() - t0, 3)
     n_full = len(full.items)
-    del per_item, plain_full
+    del per_item, stacked, plain_full
     torch.cuda.empty_cache()
     slices = b.sample.grid.shape[0]
     res = {"case": f"{items} of 1024 items, sizes {b.info['sizes']}, {slices} slices each",
@@ -549,8 +553,10 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
            "graph_capture_s": round(capture_s, 2), **out,
            "full_batch": {"items": n_full,
                           "fused_items_per_s": round(n_full / full_out["fused_s"], 2),
+                          "fused_stacked_items_per_s": round(n_full / full_out["fused_stacked_s"], 2),
                           "plain_loop_items_per_s": round(n_full / full_out["plain_loop_s"], 2),
-                          "speedup": round(full_out["plain_loop_s"] / full_out["fused_s"], 2),
+                          "speedup": round(full_out["plain_loop_s"] /
+                                           min(full_out["fused_s"], full_out["fused_stacked_s"]), 2),
                           **full_out}}
     return res
 
