@@ -1,13 +1,29 @@
-"""Generate tests/golden/setup_ref/: a simulation directory prepared by big-wave's own
-setup_simulation (big-wave/multisim.py:727-1397) for a 256 x 256 run with one voxel sample and
-five point sources (uniform energies in 15-30 keV, Gaussian source positions, seed 42), so the
-tests can check this package's source sampling and its parsing of a real prepared directory.
+"""Generate the simulation directories under tests/golden/ that big-wave's own setup_simulation
+(big-wave/multisim.py:727-1399) prepares, so the tests can check this package's source sampling,
+its parsing of a prepared directory, and its own setup_simulation file by file:
+
+* setup_ref/: 256 x 256, one voxel sample (W, Au), five point sources (uniform energies in
+  15-30 keV, Gaussian source positions, seed 42);
+* setup_ref_plasma/: 512 x 512 (nx from N / ny), a voxel sample then a plasma sample with a formula and one with a
+  bare Z, chunk_size "auto" under a 2 GB runtime budget, c16, the detector directly behind the
+  last element (the cutoff-angle rule for a last leg that is never propagated), three sources;
+* setup_ref_fresnel/: 256 x 256 with use_fresnel_scaling and one voxel sample, the detector
+  larger than the grid (the similarity frame), four sources;
+* setup_ref_exit/: a voxel sample followed by a save_and_exit marker and a second sample (the
+  element list cut at the marker, the detector moved to it), two sources.
 
 big-wave needs two things this container does not have, which the script supplies:
 * ruamel.yaml: config.load / config.save go through a stand-in backed by this package's
   yaml_io (so the YAML text is yaml_io's; the values are big-wave's);
-* nist_lookup's xray_delta_beta (sqlalchemy): the delta-beta tables come from the Chantler
-  restatement in chantler_constants.py over nist_lookup's own xrayref.db.
+* SQLAlchemy, under nist_lookup's database layer: the minimal stand-in of
+  make_chantler_golden.py, so nist_lookup's own xray_delta_beta and big-wave's own plasma
+  scattering factors run unmodified over nist_lookup's xrayref.db.
+
+computed.yaml's provenance.git_commit (the reference checkout's revision) is replaced by
+"reference" so the fixtures do not depend on the checkout. big-wave then runs source 0 of the
+plasma, Fresnel and save_and_exit directories with its own run_single_simulation (NumPy, the
+configured dtype); setup_runs.npz keeps their detector images and, for save_and_exit, every
+fourth row and column of the field it saved.
 
     python tests/golden/make_setup_golden.py [/path/to/RAVE-SIM]
 """
@@ -15,35 +31,18 @@ from __future__ import annotations
 
 import importlib
 import shutil
-import sqlite3
 import sys
 import tempfile
 from pathlib import Path
 
-import numpy as np
-
 HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
 sys.path.insert(0, str(HERE.parents[1]))
-from chantler_constants import delta_beta  # noqa: E402
+from make_chantler_golden import _fake_sqlalchemy  # noqa: E402
 from make_golden import import_reference  # noqa: E402
+from setup_cases import CASES, RUN_CASES, write_inputs  # noqa: E402
 
-OUT = HERE / "setup_ref"
-
-
-def config_dict() -> dict:
-    return {
-        "sim_params": {"N": 256 * 256, "nx": 256, "ny": 256, "dx": 2e-7, "dy": 2e-7, "z_detector": 1.0,
-                       "detector_size": 12.8e-6, "detector_size_x": 12.8e-6, "detector_size_y": 12.8e-6,
-                       "detector_pixel_size_x": 0.8e-6, "detector_pixel_size_y": 0.8e-6, "chunk_size": 256},
-        "elements": [{"type": "sample", "z_start": 0.5, "pixel_size_x": 4e-7, "pixel_size_y": 4e-7,
-                      "pixel_size_z": 1e-6, "grid_path": "grid.npy",
-                      "materials": [["W", 19.3], ["Au", 19.32]], "x_positions": [0.0],
-                      "y_positions": [0.0]}],
-        "dtype": "c8",
-        "multisource": {"type": "points", "nr_source_points": 5, "energy_range": [15000.0, 30000.0],
-                        "x_range": [-2e-6, 2e-6], "y_range": [-1e-6, 1e-6], "z": 0.0, "seed": 42},
-    }
+import numpy as np  # noqa: E402
 
 
 def main(root: Path) -> None:
@@ -65,23 +64,32 @@ def main(root: Path) -> None:
             f.write(yio.dumps(dct))
 
     bw_config.YAML = YamlStandIn
-    db = sqlite3.connect(f"file:{root / 'nist_lookup' / 'nist_lookup' / 'xrayref.db'}?mode=ro", uri=True)
-
-    def xray_delta_beta(material, density, energy, *a, **k):
-        d, b = delta_beta(db, {material: 1}, density, energy)
-        return d, b, None
-
-    oe.xray_delta_beta = xray_delta_beta
-    rng = np.random.default_rng(3)
+    sys.modules.update(_fake_sqlalchemy())
+    sys.modules.pop("nist_lookup.xraydb_plugin", None)  # the stub import_reference put there
+    real = importlib.import_module("nist_lookup.xraydb_plugin")
+    oe.xray_delta_beta = real.xray_delta_beta
+    ms._git_commit = lambda: "reference"
+    runs: dict = {}
     with tempfile.TemporaryDirectory() as tmp:
         tmp = Path(tmp)
-        grid = rng.integers(0, 3, size=(4, 12, 12), dtype=np.uint32)
-        np.save(tmp / "grid.npy", grid)
-        sim = ms.setup_simulation(config_dict(), tmp, tmp / "out")
-        if OUT.exists():
-            shutil.rmtree(OUT)
-        shutil.copytree(sim, OUT)
-    print("wrote", OUT)
+        write_inputs(tmp)
+        for name, make in CASES.items():
+            sim = ms.setup_simulation(make(), tmp, tmp / f"out_{name}")
+            out = HERE / name
+            if out.exists():
+                shutil.rmtree(out)
+            shutil.copytree(sim, out)
+            print("wrote", out)
+            if name in RUN_CASES:
+                # big-wave runs source 0 of the directory it prepared (its own NumPy path)
+                ms.run_single_simulation(sim, 0, tmp / f"scratch_{name}")
+                runs[f"{name}_detected"] = np.load(sim / "00000000" / "detected.npy")
+                u_file = sim / "00000000" / "u_0000.npy"
+                if u_file.exists():
+                    n = CASES[name]()["sim_params"]
+                    runs[f"{name}_u_sub"] = np.load(u_file).reshape(n["ny"], n["nx"])[::4, ::4].copy()
+    np.savez(HERE / "setup_runs.npz", **runs)
+    print("wrote", HERE / "setup_runs.npz", sorted(runs))
 
 
 if __name__ == "__main__":
