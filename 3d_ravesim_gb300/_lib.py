@@ -188,10 +188,10 @@ class Plan:
 
     def schedules(self) -> list[int]:
         """The schedule masks that are distinct for this plan's sizes."""
-        buf = (c_int * 64)()
+        buf = (c_int * 256)()
         n = c_int(0)
-        check(lib().rs_plan_schedules(self.handle, buf, 64, ctypes.byref(n)), "rs_plan_schedules")
-        return [buf[i] for i in range(min(n.value, 64))]
+        check(lib().rs_plan_schedules(self.handle, buf, 256, ctypes.byref(n)), "rs_plan_schedules")
+        return [buf[i] for i in range(min(n.value, 256))]
 
     def status(self) -> int:
         """Synchronise and return the device status word (0 = no bounded wait gave up)."""

@@ -133,8 +133,9 @@ def tune_multislice(nx: int, ny: int, device: torch.device | str = "cuda", slice
     fastest of those that reproduce the first schedule's field."""
     from . import _lib
     device = torch.device(device)
-    if slices is None:  # about 4 slices' worth of a 4096^2 grid, at least 2, at most 16
-        slices = int(max(2, min(16, (4 * 4096 * 4096) // (nx * ny))))
+    if slices is None:  # 16 slices' worth of a 4096^2 grid, at least 2, at most 16: per-slice
+        # differences of a few microseconds then outweigh the run's fixed start and end
+        slices = int(max(2, min(16, (16 * 4096 * 4096) // (nx * ny))))
     if plan is None:
         _tuning.active = True
         try:

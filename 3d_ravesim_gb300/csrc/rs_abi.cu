@@ -141,12 +141,17 @@ struct rs_plan {
   // Split-pair multislice passes (rs_x2.cuh): kDitherTables dithered copies of the row stage table
   // and of the two-level column table, and the matching DFT constants; slice k uses copy k mod K.
   // schedule: cleared by RS_SCHED_COMP_ROWS / RS_SCHED_COMP_COLS; the default runs the split-pair
-  // column passes and the single-sequence rows (measured faster rows at 2048^2 and 4096^2)
-  bool x2r_on = false, x2c_on = true;
+  // column passes and the dithered rows one row per thread group (4096^2 row pass: 127 us against
+  // 142 us with compensated twiddles and 158 us as split pairs)
+  bool x2r_on = true, x2c_on = true;
   bool x2_rows = false, x2_cols = false;  // available for this plan's sizes
+  bool d1_rows = true;                    // dithered rows one per thread group (RS_SCHED_SINGLE_ROWS)
+  bool d1_cols = false;                   // dithered columns one per thread group (RS_SCHED_SINGLE_COLS)
   void* twd_arena = nullptr;
   float4* twd_x = nullptr;
   float4* twd_y2 = nullptr;
+  float2* twd1_x = nullptr;               // twd_x as (wr, wi) entries, for the single-sequence rows
+  float2* twd1_y2 = nullptr;              // twd_y2 likewise, for the single-sequence columns
   int twd_x_len = 0, twd_y2_len = 0;
   DftConsts kconst[kDitherTables];
   struct MapEntry {
@@ -359,7 +364,10 @@ cudaError_t run_col_ms(rs_plan* p, const ColArgs& ca, int j, bool* used, cudaStr
   int w = 0, bh = 0;
   const int depth = ca.batches > 1 ? ca.batches : 1;
   const bool dense = depth == 1 || ca.bstride == static_cast<long long>(p->nx) * p->ny;
-  if (p->x2c_on && p->x2_cols && dense && ca.pitch == 0 && ca.tw4 == 0 && !ca.kyi && col_x2_box(p->ny, &w, &bh) &&
+  // dithered columns: split pairs (col_x2_box strips) or one column per thread group
+  // (col_pipe_box strips), the same values
+  const bool boxed = p->d1_cols ? col_pipe_box(p->ny, &w, &bh) : col_x2_box(p->ny, &w, &bh);
+  if (p->x2c_on && p->x2_cols && dense && ca.pitch == 0 && ca.tw4 == 0 && !ca.kyi && boxed &&
       aligned16(ca.in) && aligned16(ca.out) && tensor_map_encoder()) {
     const CUtensorMap* mi = field_map(p, ca.in, w, bh, depth);
     if (mi) {
@@ -368,12 +376,14 @@ cudaError_t run_col_ms(rs_plan* p, const ColArgs& ca, int j, bool* used, cudaStr
       if (mo) {
         ColArgs c = ca;
         c.twd = p->twd_y2 + static_cast<size_t>(j) * p->twd_y2_len;
+        c.twd1 = p->twd1_y2 + static_cast<size_t>(j) * p->twd_y2_len;
         c.kc = p->kconst[j];
         c.test_stall = p->test_stall;
         p->test_stall = 0;
         p->status_pending = true;
         *used = true;
-        return launch_col_x2(p->ny, c, in_copy, *mo, p->status, s);
+        return p->d1_cols ? launch_col_d1(p->ny, c, in_copy, *mo, p->status, s)
+                          : launch_col_x2(p->ny, c, in_copy, *mo, p->status, s);
       }
     }
   }
@@ -558,6 +568,21 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
   const bool plasma_rows_vox = !src.plasma || (p->fast && p->row_vox && !src.store);
   const bool x2r = p->fast && p->x2r_on && p->x2_rows && plasma_rows_vox && g->nx_v <= row_x2_slots(p->nx);
   auto table_x = [&](int z) { return p->twd_x + static_cast<size_t>(z % kDitherTables) * p->twd_x_len; };
+  auto table1_x = [&](int z) { return p->twd1_x + static_cast<size_t>(z % kDitherTables) * p->twd_x_len; };
+  // the dithered rows, as split pairs or one row per thread group (the same values)
+  auto launch_rows_dith = [&](RowArgs& r, int z_fwd, int z_inv, cudaStream_t st) {
+    if (z_fwd >= 0) {
+      r.twd_fwd = table_x(z_fwd);
+      r.twd1_fwd = table1_x(z_fwd);
+      r.k_fwd = p->kconst[z_fwd % kDitherTables];
+    }
+    if (z_inv >= 0) {
+      r.twd_inv = table_x(z_inv);
+      r.twd1_inv = table1_x(z_inv);
+      r.k_inv = p->kconst[z_inv % kDitherTables];
+    }
+    return p->d1_rows ? launch_row_d1(p->nx, r, st) : launch_row_x2(p->nx, r, st);
+  };
   double cur_dz = NAN, cur_cs = NAN;
   for (int z = s0; z < s1; ++z) {
     const double dz = slice_dz[z];
@@ -621,13 +646,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       r.pl = pl;
       const int er = prof_begin(p, 0, s);
       if (x2r) {
-        r.twd_fwd = table_x(z);
-        r.k_fwd = p->kconst[z % kDitherTables];
-        if (z != s0) {
-          r.twd_inv = table_x(z - 1);
-          r.k_inv = p->kconst[(z - 1) % kDitherTables];
-        }
-        RS_CK(launch_row_x2(p->nx, r, s));
+        RS_CK(launch_rows_dith(r, z, z != s0 ? z - 1 : -1, s));
       } else {
         RS_CK(run_row(p, r, s));
       }
@@ -653,9 +672,7 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
     RowArgs r{};
     r.in = u; r.out = u; r.ny = p->ny * src.batch; r.tw = p->tws_x; r.flags = ROW_INV;
     if (x2r) {
-      r.twd_inv = table_x(s1 - 1);
-      r.k_inv = p->kconst[(s1 - 1) % kDitherTables];
-      RS_CK(launch_row_x2(p->nx, r, s));
+      RS_CK(launch_rows_dith(r, -1, s1 - 1, s));
     } else {
       RS_CK(run_row(p, r, s));
     }
@@ -944,12 +961,16 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
     p->twd_y2_len = p->x2_cols ? static_cast<int>(tw2y) : 0;
     const size_t n = static_cast<size_t>(p->twd_x_len + p->twd_y2_len) * kDitherTables;
     if (n > 0) {
-      e = counted_malloc(&p->twd_arena, n * sizeof(float4));
+      // the split-pair (wr, wr, wi, wi) tables, then the same entries as (wr, wi)
+      e = counted_malloc(&p->twd_arena, n * (sizeof(float4) + sizeof(float2)));
       if (e == cudaSuccess) {
         p->twd_x = static_cast<float4*>(p->twd_arena);
         p->twd_y2 = p->twd_x + static_cast<size_t>(p->twd_x_len) * kDitherTables;
+        p->twd1_x = reinterpret_cast<float2*>(p->twd_x + n);
+        p->twd1_y2 = p->twd1_x + static_cast<size_t>(p->twd_x_len) * kDitherTables;
         if (p->x2_rows) e = launch_dither_tables(p->tws_x, p->twd_x, p->twd_x_len, 0);
         if (e == cudaSuccess && p->x2_cols) e = launch_dither_tables(p->tw2_y, p->twd_y2, p->twd_y2_len, 0);
+        if (e == cudaSuccess) e = launch_single_tables(p->twd_x, p->twd1_x, n, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
       }
       if (e != cudaSuccess) {
@@ -997,9 +1018,11 @@ int rs_plan_set_pipeline(rs_plan* p, int mask) {
 int rs_plan_set_schedule(rs_plan* p, int mask) {
   RS_TRY(check_plan(p));
   if (mask & ~(RS_SCHED_PIPE_ROWS | RS_SCHED_PIPE_COLS | RS_SCHED_ROW_GENERAL | RS_SCHED_SPLIT_COLS |
-               RS_SCHED_COMP_ROWS | RS_SCHED_COMP_COLS))
+               RS_SCHED_COMP_ROWS | RS_SCHED_COMP_COLS | RS_SCHED_SINGLE_ROWS | RS_SCHED_SINGLE_COLS))
     return fail(RS_EINVAL, "unknown schedule bits 0x%x", mask);
   p->x2r_on = (mask & RS_SCHED_COMP_ROWS) == 0;
+  p->d1_rows = (mask & RS_SCHED_SINGLE_ROWS) != 0;
+  p->d1_cols = (mask & RS_SCHED_SINGLE_COLS) != 0;
   p->x2c_on = (mask & RS_SCHED_COMP_COLS) == 0;
   p->pipe_rows = (mask & RS_SCHED_PIPE_ROWS) != 0;
   p->pipe_cols = (mask & RS_SCHED_PIPE_COLS) != 0;
@@ -1013,7 +1036,8 @@ int rs_plan_get_schedule(const rs_plan* p, int* mask) {
   if (!mask) return fail(RS_EINVAL, "mask is NULL");
   *mask = (p->pipe_rows ? RS_SCHED_PIPE_ROWS : 0) | (p->pipe_cols ? RS_SCHED_PIPE_COLS : 0) |
           (p->row_vox ? 0 : RS_SCHED_ROW_GENERAL) | (p->split_cols ? RS_SCHED_SPLIT_COLS : 0) |
-          (p->x2r_on ? 0 : RS_SCHED_COMP_ROWS) | (p->x2c_on ? 0 : RS_SCHED_COMP_COLS);
+          (p->x2r_on ? 0 : RS_SCHED_COMP_ROWS) | (p->x2c_on ? 0 : RS_SCHED_COMP_COLS) |
+          (p->d1_rows ? RS_SCHED_SINGLE_ROWS : 0) | (p->d1_cols ? RS_SCHED_SINGLE_COLS : 0);
   return RS_OK;
 }
 
@@ -1026,7 +1050,10 @@ int rs_plan_schedules(const rs_plan* p, int* masks, int cap, int* count) {
   const bool rows_pipe = p->fast && row_pipe_ok(p->nx);
   const bool cols_pipe = p->fast && col_pipe_box(p->ny, &w, &bh);
   int n = 0;
-  for (int m = 0; m < 64; ++m) {
+  for (int m = 0; m < 256; ++m) {
+    // one row (column) per thread group is a variant of the dithered (split-pair) rows (columns) only
+    if ((m & RS_SCHED_SINGLE_ROWS) && ((m & RS_SCHED_COMP_ROWS) || !p->x2_rows)) continue;
+    if ((m & RS_SCHED_SINGLE_COLS) && ((m & RS_SCHED_COMP_COLS) || !p->x2_cols)) continue;
     // a direction without split-pair passes has only its single-sequence kernels; where the
     // split-pair passes run, the bits that choose among that direction's other kernels change nothing
     if ((m & RS_SCHED_COMP_ROWS) && !p->x2_rows) continue;

@@ -116,9 +116,11 @@ __device__ __forceinline__ void dft_all(float2 (&v)[E], std::integer_sequence<in
 // table in shared memory (a generic pointer into the block's shared window).
 struct TwGlobal {
   static __device__ __forceinline__ float4 load(const float4* p) { return __ldg(p); }
+  static __device__ __forceinline__ float2 load(const float2* p) { return __ldg(p); }
 };
 struct TwShared {
   static __device__ __forceinline__ float4 load(const float4* p) { return *p; }
+  static __device__ __forceinline__ float2 load(const float2* p) { return *p; }
 };
 
 // WARP = false: the sequence spans the block; each exchange is write, barrier, read, barrier.

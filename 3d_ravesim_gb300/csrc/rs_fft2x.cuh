@@ -19,6 +19,12 @@
 // K slices is zero to 1/(2K) ulp; a float32 emulation of 514 slices at K = 64 gives the same
 // intensity error as exact twiddles (1.05e-5 vs 1.06e-5; 7.4e-5 with fixed rounded twiddles).
 // A table entry holds its twiddle as (wr, wr, wi, wi): both sequences' multiplier pairs.
+//
+// Single-sequence form. The same butterflies, stage structure and tables also run on one sequence
+// per thread group (value type float2 = (re, im), tables of (wr, wi) entries, DftK1 constants):
+// every add, subtract and product there is the operation its split-pair counterpart applies to
+// each lane, in the same order, so a single-sequence transform gives the bits of the split-pair
+// one (up to the sign of zero) with half the registers per thread.
 #pragma once
 #include "rs_fft.cuh"
 
@@ -54,14 +60,14 @@ __device__ __forceinline__ cp2 x_mul3(cp2 a, float2 wr, float2 wi, float2 nwi) {
 }
 // Per-lane product a * h, h = (HR, HI) holding a different multiplier for each sequence.
 __device__ __forceinline__ cp2 x_mul_pair(cp2 a, cp2 h) {
-  const float2 nhi = p_sub(make_float2(0.f, 0.f), h.im);
+  const float2 nhi = make_float2(-h.im.x, -h.im.y);
   return {p_fma(a.re, h.re, p_mul(a.im, nhi)), p_fma(a.im, h.re, p_mul(a.re, h.im))};
 }
 // Table twiddle w = (wr, wr, wi, wi): forward a * w, inverse a * conj(w).
 template <bool INV>
 __device__ __forceinline__ cp2 x_mul_tw(cp2 a, float4 w) {
   const float2 wr = make_float2(w.x, w.y), wi = make_float2(w.z, w.w);
-  const float2 nwi = p_sub(make_float2(0.f, 0.f), wi);
+  const float2 nwi = make_float2(-w.z, -w.w);
   return INV ? x_mul3(a, wr, nwi, wi) : x_mul3(a, wr, wi, nwi);
 }
 
@@ -77,6 +83,68 @@ __device__ __forceinline__ DftK dft_k(const DftConsts& k) {
   return {make_float2(k.c8, k.c8), make_float2(-k.c8, -k.c8), make_float2(k.s8, k.s8),
           make_float2(-k.s8, -k.s8), make_float2(k.r2, k.r2), make_float2(-k.r2, -k.r2)};
 }
+
+// ---- single-sequence form: the lane operations above on one (re, im) value
+struct DftK1 {
+  float c8, s8, r2;
+};
+__device__ __forceinline__ DftK1 dft_k1(const DftConsts& k) { return {k.c8, k.s8, k.r2}; }
+
+__device__ __forceinline__ float2 x_add(float2 a, float2 b) { return p_add(a, b); }
+__device__ __forceinline__ float2 x_sub(float2 a, float2 b) { return p_sub(a, b); }
+template <bool INV>
+__device__ __forceinline__ float2 x_add_rot(float2 a, float2 b) {
+  return INV ? make_float2(a.x - b.y, a.y + b.x) : make_float2(a.x + b.y, a.y - b.x);
+}
+template <bool INV>
+__device__ __forceinline__ float2 x_sub_rot(float2 a, float2 b) {
+  return INV ? make_float2(a.x + b.y, a.y - b.x) : make_float2(a.x - b.y, a.y + b.x);
+}
+// a * (wr + i wi) with nwi = -wi: re = fma(re, wr, im * nwi), im = fma(im, wr, re * wi)
+__device__ __forceinline__ float2 x_mul3(float2 a, float wr, float wi, float nwi) {
+  return make_float2(fmaf(a.x, wr, a.y * nwi), fmaf(a.y, wr, a.x * wi));
+}
+// Table twiddle w = (wr, wi): forward a * w, inverse a * conj(w).
+template <bool INV>
+__device__ __forceinline__ float2 x_mul_tw(float2 a, float2 w) {
+  return INV ? x_mul3(a, w.x, -w.y, w.y) : x_mul3(a, w.x, w.y, -w.y);
+}
+// a * h for a transmission factor h = (Re, Im), as x_mul_pair forms each lane.
+__device__ __forceinline__ float2 x_mul_one(float2 a, float2 h) { return x_mul3(a, h.x, h.y, -h.y); }
+
+template <int M, bool INV>
+__device__ __forceinline__ float2 tw16x(float2 a, const DftK1& k) {
+  if constexpr (M == 0) {
+    return a;
+  } else if constexpr (M == 2) {
+    return INV ? make_float2((a.x - a.y) * k.r2, (a.x + a.y) * k.r2)
+               : make_float2((a.x + a.y) * k.r2, (a.y - a.x) * k.r2);
+  } else if constexpr (M == 6) {
+    return INV ? make_float2((a.x + a.y) * -k.r2, (a.x - a.y) * k.r2)
+               : make_float2((a.y - a.x) * k.r2, (a.x + a.y) * -k.r2);
+  } else if constexpr (M == 1) {
+    return INV ? x_mul3(a, k.c8, k.s8, -k.s8) : x_mul3(a, k.c8, -k.s8, k.s8);
+  } else if constexpr (M == 3) {
+    return INV ? x_mul3(a, k.s8, k.c8, -k.c8) : x_mul3(a, k.s8, -k.c8, k.c8);
+  } else {
+    static_assert(M == 9, "W16 power");
+    return INV ? x_mul3(a, -k.c8, -k.s8, k.s8) : x_mul3(a, -k.c8, k.s8, -k.s8);
+  }
+}
+
+// Value type -> its twiddle-table entry and DFT-constant types.
+template <class V>
+struct XForm;
+template <>
+struct XForm<cp2> {
+  using Tw = float4;
+  using K = DftK;
+};
+template <>
+struct XForm<float2> {
+  using Tw = float2;
+  using K = DftK1;
+};
 
 // Multiply by W16^M = exp(-+2 pi i M/16) (M as used inside the radix-16 butterfly; M = 4 is
 // folded into the butterfly's adds).
@@ -103,33 +171,33 @@ __device__ __forceinline__ cp2 tw16x(cp2 a, const DftK& k) {
 }
 
 // 4-point DFT in place; ROT2: a2 arrives still to be multiplied by -i (forward) / +i (inverse).
-template <bool INV, bool ROT2 = false>
-__device__ __forceinline__ void dft4x(cp2& a0, cp2& a1, cp2& a2, cp2& a3) {
-  const cp2 t0 = ROT2 ? x_add_rot<INV>(a0, a2) : x_add(a0, a2);
-  const cp2 t1 = ROT2 ? x_sub_rot<INV>(a0, a2) : x_sub(a0, a2);
-  const cp2 t2 = x_add(a1, a3);
-  const cp2 d = x_sub(a1, a3);
+template <bool INV, bool ROT2 = false, class V>
+__device__ __forceinline__ void dft4x(V& a0, V& a1, V& a2, V& a3) {
+  const V t0 = ROT2 ? x_add_rot<INV>(a0, a2) : x_add(a0, a2);
+  const V t1 = ROT2 ? x_sub_rot<INV>(a0, a2) : x_sub(a0, a2);
+  const V t2 = x_add(a1, a3);
+  const V d = x_sub(a1, a3);
   a0 = x_add(t0, t2);
   a2 = x_sub(t0, t2);
   a1 = x_add_rot<INV>(t1, d);
   a3 = x_sub_rot<INV>(t1, d);
 }
 
-template <bool INV>
-__device__ __forceinline__ void dft2x(cp2& a0, cp2& a1) {
-  const cp2 t = a0;
+template <bool INV, class V>
+__device__ __forceinline__ void dft2x(V& a0, V& a1) {
+  const V t = a0;
   a0 = x_add(t, a1);
   a1 = x_sub(t, a1);
 }
 
 // Natural order in and out.
-template <bool INV>
-__device__ __forceinline__ void dft8x(cp2 (&a)[8], const DftK& k) {
+template <bool INV, class V, class K>
+__device__ __forceinline__ void dft8x(V (&a)[8], const K& k) {
   dft4x<INV>(a[0], a[2], a[4], a[6]);
   dft4x<INV>(a[1], a[3], a[5], a[7]);
   a[3] = tw16x<2, INV>(a[3], k);  // W8^1
   a[7] = tw16x<6, INV>(a[7], k);  // W8^3; W8^2 of a[5] folded below
-  cp2 y[8];
+  V y[8];
   y[0] = x_add(a[0], a[1]);
   y[4] = x_sub(a[0], a[1]);
   y[1] = x_add(a[2], a[3]);
@@ -143,8 +211,8 @@ __device__ __forceinline__ void dft8x(cp2 (&a)[8], const DftK& k) {
 }
 
 // 16-point DFT as 4 x 4 (as dft16 of rs_common.cuh), natural order in and out.
-template <bool INV>
-__device__ __forceinline__ void dft16x(cp2 (&a)[16], const DftK& k) {
+template <bool INV, class V, class K>
+__device__ __forceinline__ void dft16x(V (&a)[16], const K& k) {
 #pragma unroll
   for (int r2 = 0; r2 < 4; ++r2) dft4x<INV>(a[r2], a[4 + r2], a[8 + r2], a[12 + r2]);
   a[5] = tw16x<1, INV>(a[5], k);
@@ -159,7 +227,7 @@ __device__ __forceinline__ void dft16x(cp2 (&a)[16], const DftK& k) {
   dft4x<INV>(a[4], a[5], a[6], a[7]);
   dft4x<INV, true>(a[8], a[9], a[10], a[11]);
   dft4x<INV>(a[12], a[13], a[14], a[15]);
-  cp2 y[16];
+  V y[16];
 #pragma unroll
   for (int k1 = 0; k1 < 4; ++k1)
 #pragma unroll
@@ -168,13 +236,13 @@ __device__ __forceinline__ void dft16x(cp2 (&a)[16], const DftK& k) {
   for (int i = 0; i < 16; ++i) a[i] = y[i];
 }
 
-template <int R, bool INV, int OFF>
-__device__ __forceinline__ void dft_slice2x(cp2 (&v)[16], const DftK& k) {
+template <int R, bool INV, int OFF, class V, class K>
+__device__ __forceinline__ void dft_slice2x(V (&v)[16], const K& k) {
   if constexpr (R == 16) {
     static_assert(OFF == 0, "radix-16 stages use the whole array");
     dft16x<INV>(v, k);
   } else if constexpr (R == 8) {
-    cp2 a[8];
+    V a[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) a[i] = v[OFF + i];
     dft8x<INV>(a, k);
@@ -187,20 +255,23 @@ __device__ __forceinline__ void dft_slice2x(cp2 (&v)[16], const DftK& k) {
   }
 }
 
-template <int R, bool INV, int... Bs>
-__device__ __forceinline__ void dft_all2x(cp2 (&v)[16], const DftK& k, std::integer_sequence<int, Bs...>) {
+template <int R, bool INV, class V, class K, int... Bs>
+__device__ __forceinline__ void dft_all2x(V (&v)[16], const K& k, std::integer_sequence<int, Bs...>) {
   (dft_slice2x<R, INV, Bs * R>(v, k), ...);
 }
 
-// Stockham stages of FftPlan<N> (powers of two: 16 values per thread) on split pairs; the same
-// stage structure, register mappings and exchange addressing as FftStages, with the exchange
-// buffer holding one cp2 (16 bytes) per position. tw: this table's stage-major dithered entries.
-template <int N, bool INV, int SI, int NS, class AD = PadAddr, bool WARP = false, class TWL = TwGlobal, int STR = 1>
+// Stockham stages of FftPlan<N> (powers of two: 16 values per thread) on split pairs (V = cp2)
+// or single sequences (V = float2); the same stage structure, register mappings and exchange
+// addressing as FftStages, with the exchange buffer holding one V per position. tw: this table's
+// stage-major dithered entries.
+template <int N, bool INV, int SI, int NS, class AD = PadAddr, bool WARP = false, class TWL = TwGlobal, int STR = 1,
+          class V = cp2>
 struct FftStages2x {
   using P = FftPlan<N>;
+  using Tw = typename XForm<V>::Tw;
+  using K = typename XForm<V>::K;
   static_assert(P::POW2, "split-pair transforms are built for power-of-two lengths");
-  static __device__ __forceinline__ void run(cp2 (&v)[16], cp2* buf, int t, const float4* __restrict__ tw,
-                                             const DftK& k) {
+  static __device__ __forceinline__ void run(V (&v)[16], V* buf, int t, const Tw* __restrict__ tw, const K& k) {
     constexpr int R = P::radix(INV, SI);
     constexpr int B = 16 / R;
     constexpr int T = P::T;
@@ -209,7 +280,7 @@ struct FftStages2x {
       for (int b = 0; b < B; ++b) {
         const int kk = (t + b * T) % NS;
         constexpr int TW_OFF = (INV ? P::INV_BASE : 0) + P::stage_offset(INV, SI);
-        const float4* tws = tw + TW_OFF + kk;
+        const Tw* tws = tw + TW_OFF + kk;
 #pragma unroll
         for (int r = 1; r < R; ++r) v[b * R + r] = x_mul_tw<INV>(v[b * R + r], TWL::load(&tws[(r - 1) * NS]));
       }
@@ -231,15 +302,15 @@ struct FftStages2x {
 #pragma unroll
       for (int e = 0; e < 16; ++e) v[e] = buf[AD::at_plus(t, pt, slot_pos<N, R2>(0, e), false) * STR];
       if constexpr (!WARP) __syncthreads();
-      FftStages2x<N, INV, SI + 1, NS * R, AD, WARP, TWL, STR>::run(v, buf, t, tw, k);
+      FftStages2x<N, INV, SI + 1, NS * R, AD, WARP, TWL, STR, V>::run(v, buf, t, tw, k);
     }
   }
 };
 
-template <int N, bool INV, class AD = PadAddr, class TWL = TwGlobal>
-__device__ __forceinline__ void fft_seq2x(cp2 (&v)[16], cp2* buf, int t, const float4* __restrict__ tw,
-                                          const DftK& k) {
-  FftStages2x<N, INV, 0, 1, AD, false, TWL>::run(v, buf, t, tw, k);
+template <int N, bool INV, class AD = PadAddr, class TWL = TwGlobal, class V>
+__device__ __forceinline__ void fft_seq2x(V (&v)[16], V* buf, int t, const typename XForm<V>::Tw* __restrict__ tw,
+                                          const typename XForm<V>::K& k) {
+  FftStages2x<N, INV, 0, 1, AD, false, TWL, 1, V>::run(v, buf, t, tw, k);
 }
 
 // Barrier of the threads that share one transform's block exchange: the whole block, or one
@@ -252,11 +323,12 @@ struct BarGroup {
   __device__ __forceinline__ void sync() const { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory"); }
 };
 
-// Two-level transform of Fft2L<N> on split pairs (the same steps and mappings as fft2l_fwd /
-// fft2l_inv); table: W_N^{c m} at (c-1)*T + m, then the T-point stage-major table.
-template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock>
-__device__ __forceinline__ void fft2l_fwd2x(cp2 (&v)[16], cp2* buf, int t, const float4* __restrict__ tw,
-                                            const DftK& k, const BAR& bar = BAR{}) {
+// Two-level transform of Fft2L<N> on split pairs or single sequences (the same steps and
+// mappings as fft2l_fwd / fft2l_inv); table: W_N^{c m} at (c-1)*T + m, then the T-point
+// stage-major table.
+template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock, class V>
+__device__ __forceinline__ void fft2l_fwd2x(V (&v)[16], V* buf, int t, const typename XForm<V>::Tw* __restrict__ tw,
+                                            const typename XForm<V>::K& k, const BAR& bar = BAR{}) {
   using F = Fft2L<N>;
   constexpr int T = F::T;
   constexpr int G = F::G;
@@ -272,18 +344,18 @@ __device__ __forceinline__ void fft2l_fwd2x(cp2 (&v)[16], cp2* buf, int t, const
   const int pg = BX::at(c * T + j);
 #pragma unroll
   for (int e = 0; e < 16; ++e) v[e] = buf[BX::at_plus(c * T + j, pg, e * G, false) * STR];
-  FftStages2x<T, false, 0, 1, AD, true, TWL, STR>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
+  FftStages2x<T, false, 0, 1, AD, true, TWL, STR, V>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
 }
 
-template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock>
-__device__ __forceinline__ void fft2l_inv2x(cp2 (&v)[16], cp2* buf, int t, const float4* __restrict__ tw,
-                                            const DftK& k, const BAR& bar = BAR{}) {
+template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock, class V>
+__device__ __forceinline__ void fft2l_inv2x(V (&v)[16], V* buf, int t, const typename XForm<V>::Tw* __restrict__ tw,
+                                            const typename XForm<V>::K& k, const BAR& bar = BAR{}) {
   using F = Fft2L<N>;
   constexpr int T = F::T;
   constexpr int G = F::G;
   const int c = t / G;
   const int j = t % G;
-  FftStages2x<T, true, 0, 1, AD, true, TWL, STR>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
+  FftStages2x<T, true, 0, 1, AD, true, TWL, STR, V>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
   __syncwarp();
   const int pg = BX::at(c * T + j);
 #pragma unroll

@@ -90,6 +90,9 @@ struct RowArgs {
   const float4* twd_inv;
   const float4* twd_fwd;
   DftConsts k_inv, k_fwd;
+  // the same dithered tables as (wr, wi) entries, for the single-sequence dithered row kernel
+  const float2* twd1_inv;
+  const float2* twd1_fwd;
 };
 
 struct ColArgs {
@@ -123,6 +126,8 @@ struct ColArgs {
   // split-pair column pass (col_x2_pipe_kernel): this slice's dithered two-level table and constants
   const float4* twd;
   DftConsts kc;
+  // the same table as (wr, wi) entries, for the dithered column pass one column per thread group
+  const float2* twd1;
 };
 
 // ----------------------------------------------------------------------------- physics
@@ -412,8 +417,13 @@ struct RowGeom {
 
 // VOX = true: the multislice hot path only (optional row IFFT, voxel transmission, row FFT, the
 // optional field store and scale), so the point-source and plasma code is not in the kernel.
-template <int N, int ROWS, bool VOX = false>
+// DITH = true (with VOX, powers of two): the transforms use the slice's dithered tables
+// (twd1_inv / twd1_fwd, k_inv / k_fwd) in the single-sequence form of the split-pair arithmetic,
+// and the transmission is applied as the split-pair row kernel applies it, so the result is that
+// of row_x2_kernel with one row per thread group.
+template <int N, int ROWS, bool VOX = false, bool DITH = false>
 __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row_pass_kernel(const RowArgs a) {
+  static_assert(!DITH || (VOX && FftPlan<N>::POW2), "dithered rows: voxel hot path, power-of-two lengths");
   using P = FftPlan<N>;
   constexpr int T = P::T;
   constexpr int RF = P::entry_radix(false);   // forward entry == inverse exit mapping
@@ -430,7 +440,7 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   float2 v[E];
 
   // Transmission row coordinates, and the prefetch of its two voxel rows (block-uniform decision).
-  const bool tmode = VOX || (flags & (ROW_TVOX | ROW_TPLASMA));
+  const bool tmode = (VOX && !DITH) || (flags & (ROW_TVOX | ROW_TPLASMA));  // DITH: also the plain inverse
   const bool vox = VOX || (flags & ROW_TVOX);
   int yi = -1;
   float fy = 0.0f;
@@ -452,7 +462,11 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
 #pragma unroll
     for (int e = 0; e < E; ++e)
       v[e] = valid ? a.in[rbase + slot_pos<N, RX>(t, e)] : make_float2(0.f, 0.f);
-    fft_seq<N, true>(v, buf, t, a.tw);
+    if constexpr (DITH) {
+      fft_seq2x<N, true>(v, buf, t, a.twd1_inv, dft_k1(a.k_inv));
+    } else {
+      fft_seq<N, true>(v, buf, t, a.tw);
+    }
   } else if (!VOX && (flags & ROW_SRC)) {
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = point_source_value(a.ps, slot_pos<N, RF>(t, e), row);
@@ -512,14 +526,25 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
       if (__any_sync(0xffffffffu, any)) {
         const float at = vox ? a.vox.a : a.pl.a;
 #pragma unroll
-        for (int i = 0; i < CH; ++i) v[c0 + i] = cmul(v[c0 + i], material_factor(d[i].x, d[i].y, at));
+        for (int i = 0; i < CH; ++i) {
+          const float2 tr = material_factor(d[i].x, d[i].y, at);
+          if constexpr (DITH) {
+            v[c0 + i] = x_mul_one(v[c0 + i], tr);
+          } else {
+            v[c0 + i] = cmul(v[c0 + i], tr);
+          }
+        }
       }
     }
     if (staged) __syncthreads();  // the forward transform reuses the buffer
   }
 
   if (flags & ROW_FWD) {
-    fft_seq<N, false>(v, buf, t, a.tw);
+    if constexpr (DITH) {
+      fft_seq2x<N, false>(v, buf, t, a.twd1_fwd, dft_k1(a.k_fwd));
+    } else {
+      fft_seq<N, false>(v, buf, t, a.tw);
+    }
     if (valid) {
 #pragma unroll
       for (int e = 0; e < E; ++e) {

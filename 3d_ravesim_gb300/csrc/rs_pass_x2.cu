@@ -69,6 +69,27 @@ cudaError_t launch_col_x2_n(const ColArgs& a, const CUtensorMap& in, const CUten
 #define RS_X2OK_CASE(N) \
   case N: return true;
 
+#define RS_D1COL_CASE(N) \
+  case N: return launch_col_pipe_n<N, true>(a, in, out, status, s);
+
+cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
+                          cudaStream_t s) {
+  switch (ny) {
+    RS_X2_COL_SIZES(RS_D1COL_CASE)
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+#define RS_D1ROW_CASE(N) \
+  case N: return launch_rows_nvd<N, true, true>(a, s);
+
+cudaError_t launch_row_d1(int nx, const RowArgs& a, cudaStream_t s) {
+  switch (nx) {
+    RS_X2_ROW_SIZES(RS_D1ROW_CASE)
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 cudaError_t launch_row_x2(int nx, const RowArgs& a, cudaStream_t s) {
   switch (nx) {
     RS_X2_ROW_SIZES(RS_X2ROW_CASE)
@@ -134,6 +155,22 @@ __global__ void dither_tables_kernel(const float4* comp, float4* out, int len) {
     const float wi = dither_pick(w.y, w.w, j, 2u * static_cast<uint32_t>(i) + 0x9e3779b9u);
     out[static_cast<size_t>(j) * len + i] = make_float4(wr, wr, wi, wi);
   }
+}
+
+// The (wr, wi) lanes of split-pair table entries (wr, wr, wi, wi): the single-sequence tables.
+__global__ void single_tables_kernel(const float4* in, float2* out, size_t n) {
+  const size_t i = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 w = in[i];
+  out[i] = make_float2(w.x, w.z);
+}
+
+cudaError_t launch_single_tables(const float4* in, float2* out, size_t n, cudaStream_t s) {
+  if (n == 0) return cudaSuccess;
+  single_tables_kernel<<<static_cast<unsigned>((n + 255) / 256), 256, 0, s>>>(in, out, n);
+  const cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) note_launch();
+  return e;
 }
 
 cudaError_t launch_dither_tables(const float4* comp, float4* out, int len, cudaStream_t s) {

@@ -20,8 +20,8 @@ constexpr int rows_per_block() {
 #ifndef RS_ROW_VOXMODE
 #define RS_ROW_VOXMODE 1
 #endif
-template <int N, bool VOX>
-cudaError_t launch_rows_nv(const RowArgs& a, cudaStream_t s) {
+template <int N, bool VOX, bool DITH>
+cudaError_t launch_rows_nvd(const RowArgs& a, cudaStream_t s) {
   constexpr int ROWS = rows_per_block<N>();
   constexpr int THREADS = ROWS * FftPlan<N>::T;
   constexpr size_t SMEM = RowGeom<N, ROWS>::SMEM;
@@ -30,17 +30,22 @@ cudaError_t launch_rows_nv(const RowArgs& a, cudaStream_t s) {
   if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
   const unsigned bit = 1u << (dev & 31);
   if (!(configured & bit)) {
-    cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<N, ROWS, VOX>,
+    cudaError_t e = cudaFuncSetAttribute(row_pass_kernel<N, ROWS, VOX, DITH>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(SMEM));
     if (e != cudaSuccess) return e;
     configured |= bit;
   }
   const int blocks = (a.ny + ROWS - 1) / ROWS;
-  row_pass_kernel<N, ROWS, VOX><<<blocks, THREADS, SMEM, s>>>(a);
+  row_pass_kernel<N, ROWS, VOX, DITH><<<blocks, THREADS, SMEM, s>>>(a);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) note_launch();
   return e;
+}
+
+template <int N, bool VOX>
+cudaError_t launch_rows_nv(const RowArgs& a, cudaStream_t s) {
+  return launch_rows_nvd<N, VOX, false>(a, s);
 }
 
 // The voxel-transmission specialisation takes the multislice hot path (flags within
@@ -208,25 +213,28 @@ cudaError_t launch_row_pipe_n(const RowArgs& a, int* status, cudaStream_t s) {
   return e;
 }
 
-template <int N>
+template <int N, bool DITH = false>
 cudaError_t launch_col_pipe_n(const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
                               cudaStream_t s) {
-  using G = ColPipeGeom<N>;
+  using G = ColPipeGeom<N, DITH>;
   static unsigned configured = 0;
   static int grid_cache[32];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
   const unsigned bit = 1u << (dev & 31);
   if (!(configured & bit)) {
-    cudaError_t e = cudaFuncSetAttribute(col_pipe_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(col_pipe_kernel<N, DITH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(G::SMEM));
-    if (e != cudaSuccess) return e;
-    grid_cache[dev & 31] = resident_grid(col_pipe_kernel<N>, G::THREADS, G::SMEM, 1 << 30);
+    if (e != cudaSuccess) {
+      cudaGetLastError();  // leave no error behind for the caller's next check
+      return e;
+    }
+    grid_cache[dev & 31] = resident_grid(col_pipe_kernel<N, DITH>, G::THREADS, G::SMEM, 1 << 30);
     configured |= bit;
   }
   const int tiles = (a.nx + G::W - 1) / G::W * (a.batches > 1 ? a.batches : 1);
   const int grid = tiles < grid_cache[dev & 31] ? tiles : grid_cache[dev & 31];
-  col_pipe_kernel<N><<<grid, G::THREADS, G::SMEM, s>>>(a, in, out, status);
+  col_pipe_kernel<N, DITH><<<grid, G::THREADS, G::SMEM, s>>>(a, in, out, status);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) note_launch();
   return e;

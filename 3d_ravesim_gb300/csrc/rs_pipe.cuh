@@ -118,7 +118,7 @@ struct RowPipeGeom {
 // Largest box height <= 256 (the tensor-copy limit) that divides n.
 constexpr int box_rows(int n, int b = 256) { return (b <= 1 || n % b == 0) ? b : box_rows(n, b - 1); }
 
-template <int N>
+template <int N, bool DITH = false>
 struct ColPipeGeom {
   static constexpr int T = FftPlan<N>::T;
 #ifndef RS_COLPIPE_THREADS
@@ -134,16 +134,20 @@ struct ColPipeGeom {
   static constexpr int TILE = W * N;
   static constexpr int THREADS = W * T;
   static constexpr bool L2 = Fft2L<N>::ok(W);                 // two-level column transforms
-  // twiddles (compensated tables) copied to shared memory when they fit
+  // twiddles (compensated tables, or with DITH the dithered (wr, wi) tables) copied to shared
+  // memory when they fit
   static constexpr int TW_LEN = L2 ? Fft2L<N>::TW_LEN : FftPlan<N>::TW_USED;
-  static constexpr size_t TW_BYTES = static_cast<size_t>(TW_LEN) * sizeof(float4);
+  static constexpr size_t TW_BYTES = static_cast<size_t>(TW_LEN) * (DITH ? sizeof(float2) : sizeof(float4));
+  static_assert(!DITH || L2, "dithered columns use the two-level transform");
   // Three tile buffers when they fit beside the twiddle tables, else two: the twiddles in shared
   // memory matter more than the third buffer (the L1 left beside three 64 KB tiles cannot hold
-  // the compensated tables of 4096-point columns).
+  // the compensated tables of 4096-point columns). With DITH the third buffer is also given up
+  // for ey in shared memory.
 #ifdef RS_COLPIPE_NB
   static constexpr int NB = RS_COLPIPE_NB;
 #else
-  static constexpr int NB = (3 * TILE * 8 + TW_BYTES + 64 <= 227 * 1024) ? 3 : 2;
+  static constexpr int NB =
+      (3 * TILE * 8 + TW_BYTES + (DITH ? N * sizeof(float2) : 0) + 64 <= 227 * 1024) ? 3 : 2;
 #endif
   static constexpr size_t TILES_BYTES = static_cast<size_t>(NB) * TILE * sizeof(float2);
 #ifndef RS_COLPIPE_TW_SMEM
@@ -308,19 +312,23 @@ __global__ void __launch_bounds__(RowPipeGeom<N>::THREADS, RowPipeGeom<N>::MINB)
 }
 
 // ------------------------------------------------------------------- column pipeline
-template <int N>
-__global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
+// DITH: the slice's dithered two-level table (twd1, kc) in the single-sequence form of the
+// split-pair arithmetic, H and the mask applied as col_x2_pipe_kernel applies them: the result is
+// that kernel's, with one column per thread group.
+template <int N, bool DITH = false>
+__global__ void __launch_bounds__(ColPipeGeom<N, DITH>::THREADS, 1)
     col_pipe_kernel(const ColArgs a, const __grid_constant__ CUtensorMap map_in,
                     const __grid_constant__ CUtensorMap map_out, int* status) {
   using P = FftPlan<N>;
-  using G = ColPipeGeom<N>;
+  using G = ColPipeGeom<N, DITH>;
+  using TwT = typename std::conditional<DITH, float2, float4>::type;
   constexpr int W = G::W;
   constexpr int E = P::E;
   constexpr int RF = P::entry_radix(false);
   constexpr uint32_t TILE_BYTES = G::TILE * 8u;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   float2* tiles = reinterpret_cast<float2*>(smem_raw);
-  float4* tw_s = reinterpret_cast<float4*>(tiles + G::NB * G::TILE);
+  TwT* tw_s = reinterpret_cast<TwT*>(tiles + G::NB * G::TILE);
   float2* ey_s = reinterpret_cast<float2*>(smem_raw + G::TILES_BYTES + (G::TW_SMEM ? G::TW_BYTES : 0));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + G::TILES_BYTES + (G::TW_SMEM ? G::TW_BYTES : 0) +
                                                (G::EY_SMEM ? G::EY_BYTES : 0));
@@ -344,12 +352,18 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
     return;
   }
 
-  const float4* tw_g = G::L2 ? a.tw2 : a.tw;
+  const TwT* tw_g;
+  if constexpr (DITH) {
+    tw_g = a.twd1;
+  } else {
+    tw_g = G::L2 ? a.tw2 : a.tw;
+  }
   if constexpr (G::TW_SMEM) {  // the block's copy of the twiddle tables (read from L2 once)
     for (int i = threadIdx.x; i < G::TW_LEN; i += blockDim.x) tw_s[i] = __ldg(&tw_g[i]);
     __syncthreads();
   }
-  const float4* tw = G::TW_SMEM ? tw_s : tw_g;
+  const TwT* tw = G::TW_SMEM ? tw_s : tw_g;
+  const DftK1 k1 = dft_k1(a.kc);  // DITH only
   using TWL = typename std::conditional<G::TW_SMEM, TwShared, TwGlobal>::type;
   // with H applied, the 1/N of the inverse is folded into ey (one product per element fewer)
   const bool fold = (flags & COL_H) && (flags & COL_SCALE) && !(flags & COL_SPEC);  // U stays unscaled
@@ -396,7 +410,9 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
     if (flags & COL_FWD) {
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = col[slot_pos<N, RF>(t, e) * W];
-      if constexpr (G::L2) {
+      if constexpr (DITH) {
+        fft2l_fwd2x<N, NatAddr, SwzAddr, TWL, W>(v, col, t, tw, k1);
+      } else if constexpr (G::L2) {
         // the block exchange writes exactly the slots this thread just read: no barrier
         fft2l_fwd<N, NatAddr, SwzAddr, W, TWL>(v, col, t, tw);
       } else {
@@ -420,7 +436,11 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
         } else if (flags & COL_H) {
           const float2 eyv =
               G::EY_SMEM ? ey_s[e * P::T + t] : (fold ? cscale(__ldg(&a.ey[fy]), a.scale) : __ldg(&a.ey[fy]));
-          v[e] = cmul(v[e], cmul(exv, eyv));
+          if constexpr (DITH) {
+            v[e] = x_mul_one(v[e], x_mul3(exv, eyv.x, eyv.y, -eyv.y));
+          } else {
+            v[e] = cmul(v[e], cmul(exv, eyv));
+          }
         }
       }
     }
@@ -436,7 +456,8 @@ __global__ void __launch_bounds__(ColPipeGeom<N>::THREADS, 1)
     }
     if (flags & COL_INV) {
       // two-level: the last exchange read exactly the slots this thread writes back
-      if constexpr (G::L2) fft2l_inv<N, NatAddr, SwzAddr, W, TWL>(v, col, t, tw);
+      if constexpr (DITH) fft2l_inv2x<N, NatAddr, SwzAddr, TWL, W>(v, col, t, tw, k1);
+      else if constexpr (G::L2) fft2l_inv<N, NatAddr, SwzAddr, W, TWL>(v, col, t, tw);
       else fft_seq<N, true, SwzAddr, W, TWL>(v, col, t, tw);
 #pragma unroll
       for (int e = 0; e < E; ++e) col[slot_pos<N, RF>(t, e) * W] = v[e];

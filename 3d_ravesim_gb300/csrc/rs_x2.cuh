@@ -11,7 +11,8 @@
 namespace rs {
 
 // exp(-2 pi i a conj(delta + i beta)) of two pixels at once, formed as material_factor does
-// (half-angle cosine and sine, amplitude 1 + expm1): returns (Re, Re) and (Im, Im) pairs.
+// (half-angle cosine and sine, amplitude 1 + expm1) with each pixel's result the bits
+// material_factor gives it: returns (Re, Re) and (Im, Im) pairs.
 __device__ __forceinline__ cp2 material_factor2(float2 dA, float2 dB, float a) {
   const float2 h = make_float2(a * dA.x, a * dB.x);
   float2 sh, ch;
@@ -38,15 +39,13 @@ __device__ __forceinline__ cp2 material_factor2(float2 dA, float2 dB, float a) {
   const float2 ns = p_mul(p_mul(make_float2(-2.f, -2.f), sh), ch);  // -sin(phi)
   const float k = -6.283185307179586f * a;
   const float2 x = make_float2(k * dA.y, k * dB.y);
-  float2 em1;
-  if (fabsf(x.x) < 0.015625f && fabsf(x.y) < 0.015625f) {
-    // Taylor series through x^4 (remainder below x^5/120 < 1e-11 |x|)
-    const float2 q = p_fma(x, make_float2(0.041666666666666667f, 0.041666666666666667f),
-                           make_float2(0.16666666666666667f, 0.16666666666666667f));
-    em1 = p_mul(x, p_fma(x, p_fma(x, q, make_float2(0.5f, 0.5f)), make_float2(1.f, 1.f)));
-  } else {
-    em1 = make_float2(expm1f(x.x), expm1f(x.y));
-  }
+  // expm1: the Taylor series through x^4 where |x| < 1/64 (remainder below x^5/120 < 1e-11 |x|),
+  // expm1f elsewhere, chosen per pixel so that a pixel's factor does not depend on its partner's
+  const float2 q = p_fma(x, make_float2(0.041666666666666667f, 0.041666666666666667f),
+                         make_float2(0.16666666666666667f, 0.16666666666666667f));
+  float2 em1 = p_mul(x, p_fma(x, p_fma(x, q, make_float2(0.5f, 0.5f)), make_float2(1.f, 1.f)));
+  if (!(fabsf(x.x) < 0.015625f)) em1.x = expm1f(x.x);
+  if (!(fabsf(x.y) < 0.015625f)) em1.y = expm1f(x.y);
   const float2 amp = p_add(make_float2(1.f, 1.f), em1);
   return {p_mul(amp, c), p_mul(amp, ns)};
 }

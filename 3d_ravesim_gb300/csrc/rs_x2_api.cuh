@@ -9,8 +9,17 @@ bool row_x2_ok(int nx);
 int row_x2_slots(int nx);
 bool col_x2_box(int ny, int* w, int* bh);
 cudaError_t launch_row_x2(int nx, const RowArgs& a, cudaStream_t s);
+// the same row pass with one row per thread group (row_pass_kernel<N, ROWS, true, true>), for the
+// row_x2_ok sizes; reads twd1_inv / twd1_fwd
+cudaError_t launch_row_d1(int nx, const RowArgs& a, cudaStream_t s);
 cudaError_t launch_col_x2(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
+                          cudaStream_t s);
+// the same column pass with one column per thread group (col_pipe_kernel<N, true>; strips and
+// boxes of col_pipe_box), for the split-pair column sizes; reads twd1 and kc
+cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
                           cudaStream_t s);
 // kDitherTables dithered copies of a compensated table of `len` entries (rs_fft2x.cuh)
 cudaError_t launch_dither_tables(const float4* comp, float4* out, int len, cudaStream_t s);
+// (wr, wi) of each of `n` split-pair entries (wr, wr, wi, wi)
+cudaError_t launch_single_tables(const float4* in, float2* out, size_t n, cudaStream_t s);
 }  // namespace rs

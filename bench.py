@@ -44,17 +44,23 @@ PUBLISHED_MS_PER_LAYER = 43.25
 # at 4096^2, from ncu captures of this workload's multislice loop (every launch is a whole-field
 # pass, so a capture of a few slices gives the per-launch figure of the full run). --dram-csv
 # replaces them with the figures of a capture given on the command line.
-NCU_DRAM_BYTES_4096 = {"row_pass_kernel": 208.5e6, "col_pipe_kernel": 215.1e6,
-                       "row_x2_kernel": 208.7e6, "col_x2_pipe_kernel": 215.1e6}
+# row_pass_kernel: the dithered rows one per thread group (the default row pass; 208.5 MB with
+# compensated twiddles too), col_pipe_kernel: the dithered columns one per thread group (215.1 MB
+# compensated), col_x2_pipe_kernel: the split-pair columns (the default column pass).
+NCU_DRAM_BYTES_4096 = {"row_pass_kernel": 208.5e6, "col_pipe_kernel": 215.2e6,
+                       "row_x2_kernel": 208.7e6, "col_x2_pipe_kernel": 212.1e6}
 
 
 def pass_kernels(mask: int, n: int) -> dict:
     """Kernel that runs the multislice row / column passes of an n x n plan under a schedule mask."""
     x2_rows = n in (256, 512, 1024, 2048, 4096, 8192)
     x2_cols = n in (256, 512, 1024, 2048, 4096)
-    rows = "row_x2_kernel" if (x2_rows and not mask & 16) else ("row_pipe_kernel" if mask & 1 else "row_pass_kernel")
+    if x2_rows and not mask & 16:
+        rows = "row_pass_kernel" if mask & 64 else "row_x2_kernel"  # 64: dithered, one row per group
+    else:
+        rows = "row_pipe_kernel" if mask & 1 else "row_pass_kernel"
     if x2_cols and not mask & 32:
-        cols = "col_x2_pipe_kernel"
+        cols = "col_pipe_kernel" if mask & 128 else "col_x2_pipe_kernel"  # 128: dithered, one column per group
     else:
         cols = "col_pipe_kernel" if mask & 2 and not mask & 8 else "col_pass_kernel"
     return {"row_pass": rows, "col_pass": cols}
@@ -209,15 +215,18 @@ def l2_flush_buffer(torch, device):
 def schedule_name(mask: int) -> str:
     """Readable form of a pass-schedule mask (bits: 1 pipelined rows, 2 pipelined columns,
     4 general row kernel, 8 split columns, 16 / 32 single-sequence compensated rows / columns
-    instead of the split-pair passes, for the sizes that have them)."""
+    instead of the split-pair passes, for the sizes that have them, 64 / 128 the dithered rows /
+    columns one per thread group)."""
     if mask & 16:
         rows = "rows:pipelined" if mask & 1 else ("rows:per-block" if mask & 4 else "rows:per-block-voxel")
     else:
-        rows = "rows:split-pair"
+        rows = "rows:dithered-single" if mask & 64 else "rows:split-pair"
     if mask & 32:
         cols = "cols:pipelined" if mask & 2 else "cols:per-block"
         if mask & 8:
             cols = "cols:split-3-pass (last slice " + cols.split(":")[1] + ")"
+    elif mask & 128:
+        cols = "cols:dithered-single"
     else:
         cols = "cols:split-pair"
     return f"{rows},{cols}"

@@ -281,6 +281,15 @@ int rs_plan_set_pipeline(rs_plan* plan, int mask);
 #define RS_SCHED_COMP_ROWS 16
 #define RS_SCHED_COMP_COLS 32
 #define RS_SCHED_COMPENSATED (RS_SCHED_COMP_ROWS | RS_SCHED_COMP_COLS)
+/*   RS_SCHED_SINGLE_ROWS (without RS_SCHED_COMP_ROWS) the dithered row passes hold one row per
+ *                        thread group instead of two, in the single-sequence form of the same
+ *                        arithmetic: the same results (up to the sign of zero) with half the
+ *                        registers per thread. */
+#define RS_SCHED_SINGLE_ROWS 64
+/*   RS_SCHED_SINGLE_COLS (without RS_SCHED_COMP_COLS) the same for the dithered column passes:
+ *                        one column per thread group (the strips of the pipelined single-sequence
+ *                        column pass), the split-pair columns' results. */
+#define RS_SCHED_SINGLE_COLS 128
 int rs_plan_set_schedule(rs_plan* plan, int mask);
 int rs_plan_get_schedule(const rs_plan* plan, int* mask);
 int rs_plan_schedules(const rs_plan* plan, int* masks, int cap, int* count);

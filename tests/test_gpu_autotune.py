@@ -21,10 +21,13 @@ def test_schedule_lists(rs, cuda):
     # family (bit 16) keeps every single-sequence kernel choice
     # per direction: the split-pair passes (one schedule), or (bit 16 rows, bit 32 columns) the
     # single-sequence kernels with their own choices
+    # (bits 64 / 128: the dithered rows / columns one per thread group, where split-pair ones exist)
     assert lib.plan_for(4096, 4096, cuda).schedules() == [0, 16, 17, 20, 32, 34, 40, 42, 48, 49, 50, 51, 52, 54,
-                                                          56, 57, 58, 59, 60, 62]
-    assert lib.plan_for(2048, 2048, cuda).schedules() == [0, 16, 17, 20, 32, 34, 48, 49, 50, 51, 52, 54]  # no split
-    assert lib.plan_for(8192, 64, cuda).schedules() == [0, 16, 17, 20]  # split-pair rows, 64-point columns
+                                                          56, 57, 58, 59, 60, 62, 64, 96, 98, 104, 106,
+                                                          128, 144, 145, 148, 192]
+    assert lib.plan_for(2048, 2048, cuda).schedules() == [0, 16, 17, 20, 32, 34, 48, 49, 50, 51, 52, 54,
+                                                          64, 96, 98, 128, 144, 145, 148, 192]  # no split
+    assert lib.plan_for(8192, 64, cuda).schedules() == [0, 16, 17, 20, 64]  # split-pair rows, 64-point columns
     assert lib.plan_for(72, 40, cuda).schedules() == [0]  # direct-DFT sizes have one schedule
     p = lib.plan_for(1024, 1024, cuda)
     old = p.schedule()
@@ -32,7 +35,7 @@ def test_schedule_lists(rs, cuda):
     assert p.schedule() == 6
     p.set_schedule(old)
     with pytest.raises(Exception):
-        p.set_schedule(64)
+        p.set_schedule(256)
 
 
 @pytest.mark.parametrize("n", [1024, 1536])

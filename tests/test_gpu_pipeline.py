@@ -71,10 +71,11 @@ def test_multislice_pipeline_bit_identical(rs, cuda, n, pitch):
 
 @pytest.mark.parametrize("nx,ny", [(4096, 4096), (1024, 1536), (2048, 2048), (512, 512), (8192, 1024)])
 def test_split_pair_passes_match_compensated_passes(rs, cuda, nx, ny):
-    """The default multislice passes (two rows / two columns per thread group in packed f32x2
+    """The split-pair multislice passes (two rows / two columns per thread group in packed f32x2
     arithmetic, dithered twiddle tables) against the single-sequence passes with compensated
     twiddles on the same 12-slice voxel run: equal to FP32 rounding (both are within the FP64
-    accuracy bound; their roundings differ)."""
+    accuracy bound; their roundings differ). The dithered rows (bit 64) and columns (bit 128) one
+    per thread group give the split-pair passes' values exactly."""
     wl = rs.convert_energy_wavelength(25000.0)
     dx = 0.25e-6
     pitch = 0.7e-6
@@ -91,7 +92,7 @@ def test_split_pair_passes_match_compensated_passes(rs, cuda, nx, ny):
     old = plan.schedule()
     outs = []
     try:
-        for mask in (0, 48 | old):
+        for mask in (0, 48 | old, 64, 128):
             plan.set_schedule(mask)
             x = rng.normal(size=nx * ny) + 1j * rng.normal(size=nx * ny) if not outs else None
             if x is not None:
@@ -104,6 +105,9 @@ def test_split_pair_passes_match_compensated_passes(rs, cuda, nx, ny):
     for a, b in zip(outs[0], outs[1]):
         assert np.all(np.isfinite(a))
         assert np.linalg.norm(a - b) / np.linalg.norm(b) < 3e-6
+    for single in outs[2:]:
+        for a, b in zip(outs[0], single):
+            np.testing.assert_array_equal(a, b)
     assert plan.status() == 0
 
 
@@ -111,7 +115,8 @@ def test_split_pair_passes_match_compensated_passes(rs, cuda, nx, ny):
 def test_split_pair_rows_store_the_entering_fields(rs, cuda, n):
     """rs_multislice_dbgrid_store and rs_multislice_dbgrid_fields with the split-pair row passes
     (schedule 0) write the same fields, to FP32 rounding, as the single-sequence kernels (48), and
-    the fields-only form writes exactly what the storing forward writes."""
+    exactly the fields of the dithered rows one row per thread group (64); the fields-only form
+    writes exactly what the storing forward writes."""
     lib = rs._lib
     rng = np.random.default_rng(n)
     nz, nv = 6, n // 4 + 4
@@ -125,7 +130,7 @@ def test_split_pair_rows_store_the_entering_fields(rs, cuda, n):
     u0 = torch.polar(torch.ones(n * n), torch.from_numpy(rng.uniform(0, 6, n * n)).float()).to(torch.complex64).to(cuda)
     out = {}
     try:
-        for mask in (0, 48):
+        for mask in (0, 48, 64):
             plan.set_schedule(mask)
             for name in ("rs_multislice_dbgrid_store", "rs_multislice_dbgrid_fields"):
                 u, U = u0.clone(), torch.empty_like(u0)
@@ -137,8 +142,9 @@ def test_split_pair_rows_store_the_entering_fields(rs, cuda, n):
                 out[(mask, name)] = fields.cpu().numpy()
     finally:
         plan.set_schedule(old)
-    for mask in (0, 48):
+    for mask in (0, 48, 64):
         assert np.array_equal(out[(mask, "rs_multislice_dbgrid_store")], out[(mask, "rs_multislice_dbgrid_fields")])
+    assert np.array_equal(out[(0, "rs_multislice_dbgrid_store")], out[(64, "rs_multislice_dbgrid_store")])
     a, b = out[(0, "rs_multislice_dbgrid_store")], out[(48, "rs_multislice_dbgrid_store")]
     assert np.array_equal(a[0], b[0])  # the field entering the first slice is the input
     assert np.linalg.norm(a - b) / np.linalg.norm(b) < 3e-6
