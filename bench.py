@@ -733,9 +733,7 @@ def run_ours(args):
             "dtype": "c64 (fp32 complex)",
             "data": "synthetic (seeded Talbot-Lau: point source, gratings, 200-blob voxel sample)" if talbot else
                     "synthetic (point source 1 m upstream, seeded spherical-harmonic-perturbed CH capsule shell)",
-            "config": {"workload": f"{'talbot_lau' if talbot else 'capsule'}_{n}x{n}_c64", "nx": n, "ny": n,
-                       "slices_per_step": slices_per_step,
-                       "sample_slices": args.slices, "voxel_grid": vox, "energy_ev": w.info["energy_ev"],
+            "config": {**workload_config(w, n, slices_per_step, args.slices, vox, talbot),
                        "l2": "256 MiB buffer written between timed steps (flush outside the events)",
                        "parallelism": f"replicas x{world} (one field per GPU)"},
             "roofline": roofline, "gpu_launches": launches, "clocks": clocks.summary(),
@@ -815,10 +813,18 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def workload_config(w, n: int, slices_per_step: int, sample_slices: int, vox, talbot: bool = True) -> dict:
+    """The workload-defining part of a line's config, the same for both arms."""
+    return {"workload": f"{'talbot_lau' if talbot else 'capsule'}_{n}x{n}_c64", "nx": n, "ny": n,
+            "slices_per_step": slices_per_step, "sample_slices": sample_slices, "voxel_grid": vox,
+            "energy_ev": w.info["energy_ev"]}
+
+
 # ----------------------------------------------------------------------- reference arm
 def run_reference(args):
     """The reference's CPU algorithm (the oracle restatement of big-wave's NumpyVector path) on the
-    host cores, scipy.fft with all host threads; one step = one Sample slice-step at 4096^2 c64."""
+    host cores, scipy.fft with all host threads, on the same Talbot-Lau workload as the GPU arm;
+    one step = one Sample slice-step of it (a bounded sample of the run's 514)."""
     rank = int(os.environ.get("RANK", 0))
     if rank != 0:
         return
@@ -827,7 +833,7 @@ def run_reference(args):
     from oracle import bigwave_oracle as orc
     wlmod = importlib.import_module("3d_ravesim_gb300.workloads")
     n = args.n
-    w = wlmod.talbot_lau(n=n, slices=8, blobs=20)
+    w = wlmod.talbot_lau(n=n, slices=args.slices)
     s = w.elements[1]
     p = w.params
     grid = np.asarray(s.grid)
@@ -852,9 +858,13 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 1),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
-            "data": "synthetic", "config": {"workload": f"talbot_lau_{n}x{n}_c64", "step": "one Sample slice-step"},
+            "data": "synthetic (seeded Talbot-Lau: point source, gratings, 200-blob voxel sample)",
+            "config": {**workload_config(w, n, args.slices + 2, args.slices, w.info["voxel_grid"]),
+                       "parallelism": f"host cores x{cores}"},
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{args.steps} Sample slice-steps at {n}^2 c64, scipy.fft workers={cores}"},
+                             "sample": f"{args.steps} Sample slice-steps (sample slices 0..{args.steps - 1}, after "
+                                       f"{args.warmup} warm-up steps) of the {n}^2 c64 run, scipy.fft "
+                                       f"workers={cores}"},
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
