@@ -71,6 +71,13 @@ __device__ __forceinline__ cp2 x_mul_tw(cp2 a, float4 w) {
   return INV ? x_mul3(a, wr, nwi, wi) : x_mul3(a, wr, wi, nwi);
 }
 
+// The same product from a (wr, wi) table entry (the single-sequence layout), for split pairs
+// whose table is kept at half the size.
+template <bool INV>
+__device__ __forceinline__ cp2 x_mul_tw(cp2 a, float2 w) {
+  return x_mul_tw<INV>(a, make_float4(w.x, w.x, w.y, w.y));
+}
+
 // The real constants of the small DFTs for one table of a run: cos(pi/8), sin(pi/8) and
 // sqrt(2)/2, each dithered like the twiddle tables (host-built, one set per table).
 struct DftConsts {
@@ -265,10 +272,10 @@ __device__ __forceinline__ void dft_all2x(V (&v)[16], const K& k, std::integer_s
 // addressing as FftStages, with the exchange buffer holding one V per position. tw: this table's
 // stage-major dithered entries.
 template <int N, bool INV, int SI, int NS, class AD = PadAddr, bool WARP = false, class TWL = TwGlobal, int STR = 1,
-          class V = cp2>
+          class V = cp2, class TwT = typename XForm<V>::Tw>
 struct FftStages2x {
   using P = FftPlan<N>;
-  using Tw = typename XForm<V>::Tw;
+  using Tw = TwT;
   using K = typename XForm<V>::K;
   static_assert(P::POW2, "split-pair transforms are built for power-of-two lengths");
   static __device__ __forceinline__ void run(V (&v)[16], V* buf, int t, const Tw* __restrict__ tw, const K& k) {
@@ -302,7 +309,7 @@ struct FftStages2x {
 #pragma unroll
       for (int e = 0; e < 16; ++e) v[e] = buf[AD::at_plus(t, pt, slot_pos<N, R2>(0, e), false) * STR];
       if constexpr (!WARP) __syncthreads();
-      FftStages2x<N, INV, SI + 1, NS * R, AD, WARP, TWL, STR, V>::run(v, buf, t, tw, k);
+      FftStages2x<N, INV, SI + 1, NS * R, AD, WARP, TWL, STR, V, TwT>::run(v, buf, t, tw, k);
     }
   }
 };
@@ -326,8 +333,8 @@ struct BarGroup {
 // Two-level transform of Fft2L<N> on split pairs or single sequences (the same steps and
 // mappings as fft2l_fwd / fft2l_inv); table: W_N^{c m} at (c-1)*T + m, then the T-point
 // stage-major table.
-template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock, class V>
-__device__ __forceinline__ void fft2l_fwd2x(V (&v)[16], V* buf, int t, const typename XForm<V>::Tw* __restrict__ tw,
+template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock, class V, class TwT>
+__device__ __forceinline__ void fft2l_fwd2x(V (&v)[16], V* buf, int t, const TwT* __restrict__ tw,
                                             const typename XForm<V>::K& k, const BAR& bar = BAR{}) {
   using F = Fft2L<N>;
   constexpr int T = F::T;
@@ -344,18 +351,18 @@ __device__ __forceinline__ void fft2l_fwd2x(V (&v)[16], V* buf, int t, const typ
   const int pg = BX::at(c * T + j);
 #pragma unroll
   for (int e = 0; e < 16; ++e) v[e] = buf[BX::at_plus(c * T + j, pg, e * G, false) * STR];
-  FftStages2x<T, false, 0, 1, AD, true, TWL, STR, V>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
+  FftStages2x<T, false, 0, 1, AD, true, TWL, STR, V, TwT>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
 }
 
-template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock, class V>
-__device__ __forceinline__ void fft2l_inv2x(V (&v)[16], V* buf, int t, const typename XForm<V>::Tw* __restrict__ tw,
+template <int N, class BX, class AD, class TWL, int STR = 1, class BAR = BarBlock, class V, class TwT>
+__device__ __forceinline__ void fft2l_inv2x(V (&v)[16], V* buf, int t, const TwT* __restrict__ tw,
                                             const typename XForm<V>::K& k, const BAR& bar = BAR{}) {
   using F = Fft2L<N>;
   constexpr int T = F::T;
   constexpr int G = F::G;
   const int c = t / G;
   const int j = t % G;
-  FftStages2x<T, true, 0, 1, AD, true, TWL, STR, V>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
+  FftStages2x<T, true, 0, 1, AD, true, TWL, STR, V, TwT>::run(v, buf + BX::at(c * T) * STR, j, tw + 15 * T, k);
   __syncwarp();
   const int pg = BX::at(c * T + j);
 #pragma unroll

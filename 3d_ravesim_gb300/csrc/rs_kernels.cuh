@@ -169,6 +169,46 @@ __device__ __forceinline__ float2 material_factor(float delta, float beta, float
   return make_float2(amp * c, -amp * s);
 }
 
+// exp(-2 pi i a conj(delta + i beta)) of two pixels at once, formed as material_factor does
+// (half-angle cosine and sine, amplitude 1 + expm1) with each pixel's result the bits
+// material_factor gives it: returns (Re, Re) and (Im, Im) pairs.
+__device__ __forceinline__ cp2 material_factor2(float2 dA, float2 dB, float a) {
+  const float2 h = make_float2(a * dA.x, a * dB.x);
+  float2 sh, ch;
+  if (fabsf(h.x) < 0.0625f && fabsf(h.y) < 0.0625f) {
+    // the Taylor series of sincospi_small on both pixels at once
+    const float2 x = p_fma(h, make_float2(kPiHi, kPiHi), p_mul(h, make_float2(kPiLo, kPiLo)));
+    const float2 x2 = p_mul(x, x);
+    const float2 ps = p_fma(x2, p_fma(x2, p_fma(x2, p_fma(x2, make_float2(2.7557319e-06f, 2.7557319e-06f),
+                                                          make_float2(-1.9841270e-04f, -1.9841270e-04f)),
+                                                make_float2(8.3333333e-03f, 8.3333333e-03f)),
+                                      make_float2(-1.6666667e-01f, -1.6666667e-01f)),
+                            make_float2(1.f, 1.f));
+    sh = p_mul(x, ps);
+    ch = p_fma(x2, p_fma(x2, p_fma(x2, p_fma(x2, make_float2(2.4801587e-05f, 2.4801587e-05f),
+                                             make_float2(-1.3888889e-03f, -1.3888889e-03f)),
+                                   make_float2(4.1666667e-02f, 4.1666667e-02f)),
+                         make_float2(-0.5f, -0.5f)),
+               make_float2(1.f, 1.f));
+  } else {
+    sincospi_small(h.x, &sh.x, &ch.x);
+    sincospi_small(h.y, &sh.y, &ch.y);
+  }
+  const float2 c = p_fma(p_mul(make_float2(-2.f, -2.f), sh), sh, make_float2(1.f, 1.f));
+  const float2 ns = p_mul(p_mul(make_float2(-2.f, -2.f), sh), ch);  // -sin(phi)
+  const float k = -6.283185307179586f * a;
+  const float2 x = make_float2(k * dA.y, k * dB.y);
+  // expm1: the Taylor series through x^4 where |x| < 1/64 (remainder below x^5/120 < 1e-11 |x|),
+  // expm1f elsewhere, chosen per pixel so that a pixel's factor does not depend on its partner's
+  const float2 q = p_fma(x, make_float2(0.041666666666666667f, 0.041666666666666667f),
+                         make_float2(0.16666666666666667f, 0.16666666666666667f));
+  float2 em1 = p_mul(x, p_fma(x, p_fma(x, q, make_float2(0.5f, 0.5f)), make_float2(1.f, 1.f)));
+  if (!(fabsf(x.x) < 0.015625f)) em1.x = expm1f(x.x);
+  if (!(fabsf(x.y) < 0.015625f)) em1.y = expm1f(x.y);
+  const float2 amp = p_add(make_float2(1.f, 1.f), em1);
+  return {p_mul(amp, c), p_mul(amp, ns)};
+}
+
 // (delta, beta) of one raw voxel id (the 32-bit word as stored in the grid).
 __device__ __forceinline__ float2 db_of_id(const VoxelArgs& p, uint32_t raw) {
   int id;
@@ -525,6 +565,12 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
       }
       if (__any_sync(0xffffffffu, any)) {
         const float at = vox ? a.vox.a : a.pl.a;
+        // the factors two pixels at a time in packed arithmetic (each pixel's bits are those
+        // material_factor gives it); RS_ROW_PAIRED_FACTORS=0: one pixel at a time
+#ifndef RS_ROW_PAIRED_FACTORS
+#define RS_ROW_PAIRED_FACTORS 1
+#endif
+#if !RS_ROW_PAIRED_FACTORS
 #pragma unroll
         for (int i = 0; i < CH; ++i) {
           const float2 tr = material_factor(d[i].x, d[i].y, at);
@@ -534,6 +580,20 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
             v[c0 + i] = cmul(v[c0 + i], tr);
           }
         }
+#else
+#pragma unroll
+        for (int i = 0; i < CH; i += 2) {
+          const cp2 tr = material_factor2(d[i], d[i + 1], at);
+          const float2 t0 = make_float2(tr.re.x, tr.im.x), t1 = make_float2(tr.re.y, tr.im.y);
+          if constexpr (DITH) {
+            v[c0 + i] = x_mul_one(v[c0 + i], t0);
+            v[c0 + i + 1] = x_mul_one(v[c0 + i + 1], t1);
+          } else {
+            v[c0 + i] = cmul(v[c0 + i], t0);
+            v[c0 + i + 1] = cmul(v[c0 + i + 1], t1);
+          }
+        }
+#endif
       }
     }
     if (staged) __syncthreads();  // the forward transform reuses the buffer

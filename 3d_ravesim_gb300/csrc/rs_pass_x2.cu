@@ -30,28 +30,41 @@ cudaError_t launch_row_x2_n(const RowArgs& a, cudaStream_t s) {
   return e;
 }
 
+// Blocks per SM of the split-pair column pass: two single-buffer blocks up to 2048 rows
+// (2048^2 column pass 31.2 against 38.3 us, 1024^2 13.8 against 14.7), one block with two
+// strip buffers at 4096 (123.5 against 140.7 us: at 128 registers the 4096-point form spills).
+// RS_COLX2_MINB forces one choice for every size.
 template <int N>
+constexpr int col_x2_minb() {
+#ifdef RS_COLX2_MINB
+  return RS_COLX2_MINB;
+#else
+  return N <= 2048 ? 2 : 1;
+#endif
+}
+
+template <int N, int MINB = col_x2_minb<N>()>
 cudaError_t launch_col_x2_n(const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
                             cudaStream_t s) {
-  using G = ColX2Geom<N>;
+  using G = ColX2Geom<N, MINB>;
   static unsigned configured = 0;
   static int grid_cache[32];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
   const unsigned bit = 1u << (dev & 31);
   if (!(configured & bit)) {
-    cudaError_t e = cudaFuncSetAttribute(col_x2_pipe_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(col_x2_pipe_kernel<N, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(G::SMEM));
     if (e != cudaSuccess) {
       cudaGetLastError();
       return e;
     }
-    grid_cache[dev & 31] = resident_grid(col_x2_pipe_kernel<N>, G::THREADS, G::SMEM, 1 << 30);
+    grid_cache[dev & 31] = resident_grid(col_x2_pipe_kernel<N, MINB>, G::THREADS, G::SMEM, 1 << 30);
     configured |= bit;
   }
   const int tiles = (a.nx + G::W - 1) / G::W * (a.batches > 1 ? a.batches : 1);
   const int grid = tiles < grid_cache[dev & 31] ? tiles : grid_cache[dev & 31];
-  col_x2_pipe_kernel<N><<<grid, G::THREADS, G::SMEM, s>>>(a, in, out, status);
+  col_x2_pipe_kernel<N, MINB><<<grid, G::THREADS, G::SMEM, s>>>(a, in, out, status);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) note_launch();
   return e;

@@ -10,46 +10,6 @@
 
 namespace rs {
 
-// exp(-2 pi i a conj(delta + i beta)) of two pixels at once, formed as material_factor does
-// (half-angle cosine and sine, amplitude 1 + expm1) with each pixel's result the bits
-// material_factor gives it: returns (Re, Re) and (Im, Im) pairs.
-__device__ __forceinline__ cp2 material_factor2(float2 dA, float2 dB, float a) {
-  const float2 h = make_float2(a * dA.x, a * dB.x);
-  float2 sh, ch;
-  if (fabsf(h.x) < 0.0625f && fabsf(h.y) < 0.0625f) {
-    // the Taylor series of sincospi_small on both pixels at once
-    const float2 x = p_fma(h, make_float2(kPiHi, kPiHi), p_mul(h, make_float2(kPiLo, kPiLo)));
-    const float2 x2 = p_mul(x, x);
-    const float2 ps = p_fma(x2, p_fma(x2, p_fma(x2, p_fma(x2, make_float2(2.7557319e-06f, 2.7557319e-06f),
-                                                          make_float2(-1.9841270e-04f, -1.9841270e-04f)),
-                                                make_float2(8.3333333e-03f, 8.3333333e-03f)),
-                                      make_float2(-1.6666667e-01f, -1.6666667e-01f)),
-                            make_float2(1.f, 1.f));
-    sh = p_mul(x, ps);
-    ch = p_fma(x2, p_fma(x2, p_fma(x2, p_fma(x2, make_float2(2.4801587e-05f, 2.4801587e-05f),
-                                             make_float2(-1.3888889e-03f, -1.3888889e-03f)),
-                                   make_float2(4.1666667e-02f, 4.1666667e-02f)),
-                         make_float2(-0.5f, -0.5f)),
-               make_float2(1.f, 1.f));
-  } else {
-    sincospi_small(h.x, &sh.x, &ch.x);
-    sincospi_small(h.y, &sh.y, &ch.y);
-  }
-  const float2 c = p_fma(p_mul(make_float2(-2.f, -2.f), sh), sh, make_float2(1.f, 1.f));
-  const float2 ns = p_mul(p_mul(make_float2(-2.f, -2.f), sh), ch);  // -sin(phi)
-  const float k = -6.283185307179586f * a;
-  const float2 x = make_float2(k * dA.y, k * dB.y);
-  // expm1: the Taylor series through x^4 where |x| < 1/64 (remainder below x^5/120 < 1e-11 |x|),
-  // expm1f elsewhere, chosen per pixel so that a pixel's factor does not depend on its partner's
-  const float2 q = p_fma(x, make_float2(0.041666666666666667f, 0.041666666666666667f),
-                         make_float2(0.16666666666666667f, 0.16666666666666667f));
-  float2 em1 = p_mul(x, p_fma(x, p_fma(x, q, make_float2(0.5f, 0.5f)), make_float2(1.f, 1.f)));
-  if (!(fabsf(x.x) < 0.015625f)) em1.x = expm1f(x.x);
-  if (!(fabsf(x.y) < 0.015625f)) em1.y = expm1f(x.y);
-  const float2 amp = p_add(make_float2(1.f, 1.f), em1);
-  return {p_mul(amp, c), p_mul(amp, ns)};
-}
-
 // ------------------------------------------------------------------------------- row pass
 template <int N>
 struct RowX2Geom {
@@ -222,7 +182,10 @@ __global__ void __launch_bounds__(RowX2Geom<N>::THREADS, RowX2Geom<N>::MINB) row
 }
 
 // --------------------------------------------------------------------------- column pass
-template <int N>
+// MINB = 1: one block per SM with two or three strip buffers and the (wr, wr, wi, wi) table.
+// MINB = 2: two blocks per SM, each with one strip buffer (the other block computes while one
+// waits for its next strip), the half-size (wr, wi) table and half the register file.
+template <int N, int MINB = 1>
 struct ColX2Geom {
   using P = FftPlan<N>;
   static constexpr int T = P::T;
@@ -235,31 +198,35 @@ struct ColX2Geom {
   static constexpr int TILE = W * N;  // float2 per tile buffer
   static constexpr bool L2 = Fft2L<N>::ok(PAIRS);
   static_assert(L2, "the split-pair column pass uses the two-level transform");
+  static constexpr bool HALF_TW = MINB >= 2;
+  using TwT = typename std::conditional<HALF_TW, float2, float4>::type;
   static constexpr int TW_LEN = Fft2L<N>::TW_LEN;
-  static constexpr size_t TW_BYTES = static_cast<size_t>(TW_LEN) * sizeof(float4);
-  static constexpr int NB = (3 * TILE * 8 + TW_BYTES + 64 <= 227 * 1024) ? 3 : 2;
+  static constexpr size_t TW_BYTES = static_cast<size_t>(TW_LEN) * sizeof(TwT);
+  static constexpr size_t BUDGET = 227 * 1024 / MINB;
+  static constexpr int NB = MINB >= 2 ? 1 : (3 * TILE * 8 + TW_BYTES + 64 <= BUDGET) ? 3 : 2;
   static constexpr size_t TILES_BYTES = static_cast<size_t>(NB) * TILE * sizeof(float2);
-  static constexpr bool TW_SMEM = TILES_BYTES + TW_BYTES + 64 <= 227 * 1024;
+  static constexpr bool TW_SMEM = TILES_BYTES + TW_BYTES + 64 <= BUDGET;
   static constexpr size_t EY_BYTES = static_cast<size_t>(N) * sizeof(float2);
-  static constexpr bool EY_SMEM = TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + EY_BYTES + 64 <= 227 * 1024;
+  static constexpr bool EY_SMEM = TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + EY_BYTES + 64 <= BUDGET;
   static constexpr size_t SMEM =
       TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + (EY_SMEM ? EY_BYTES : 0) + NB * sizeof(uint64_t);
 };
 
 // Flags: COL_FWD | COL_H | COL_SCALE | COL_INV, optionally COL_SPEC (the multislice column pass).
-template <int N>
-__global__ void __launch_bounds__(ColX2Geom<N>::THREADS, 1)
+template <int N, int MINB = 1>
+__global__ void __launch_bounds__(ColX2Geom<N, MINB>::THREADS, MINB)
     col_x2_pipe_kernel(const ColArgs a, const __grid_constant__ CUtensorMap map_in,
                        const __grid_constant__ CUtensorMap map_out, int* status) {
   using P = FftPlan<N>;
-  using G = ColX2Geom<N>;
+  using G = ColX2Geom<N, MINB>;
+  using TwT = typename G::TwT;
   constexpr int W = G::W;
   constexpr int PAIRS = G::PAIRS;
   constexpr int RF = P::entry_radix(false);
   constexpr uint32_t TILE_BYTES = G::TILE * 8u;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   float2* tiles = reinterpret_cast<float2*>(smem_raw);
-  float4* tw_s = reinterpret_cast<float4*>(smem_raw + G::TILES_BYTES);
+  TwT* tw_s = reinterpret_cast<TwT*>(smem_raw + G::TILES_BYTES);
   float2* ey_s = reinterpret_cast<float2*>(smem_raw + G::TILES_BYTES + (G::TW_SMEM ? G::TW_BYTES : 0));
   uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + G::TILES_BYTES + (G::TW_SMEM ? G::TW_BYTES : 0) +
                                                (G::EY_SMEM ? G::EY_BYTES : 0));
@@ -285,10 +252,16 @@ __global__ void __launch_bounds__(ColX2Geom<N>::THREADS, 1)
     for (int kb = 0; kb < N / G::BH; ++kb)
       tma_load_3d(tiles + kb * G::BH * W, &map_in, (tile % strips) * W, kb * G::BH, tile / strips, &bars[0]);
   }
-  if constexpr (G::TW_SMEM) {
-    for (int i = threadIdx.x; i < G::TW_LEN; i += blockDim.x) tw_s[i] = __ldg(&a.twd[i]);
+  const TwT* tw_g;
+  if constexpr (G::HALF_TW) {
+    tw_g = a.twd1;
+  } else {
+    tw_g = a.twd;
   }
-  const float4* tw = G::TW_SMEM ? tw_s : a.twd;
+  if constexpr (G::TW_SMEM) {
+    for (int i = threadIdx.x; i < G::TW_LEN; i += blockDim.x) tw_s[i] = __ldg(&tw_g[i]);
+  }
+  const TwT* tw = G::TW_SMEM ? tw_s : tw_g;
   using TWL = typename std::conditional<G::TW_SMEM, TwShared, TwGlobal>::type;
   const bool fold = (flags & COL_H) && (flags & COL_SCALE) && !(flags & COL_SPEC);
   if constexpr (G::EY_SMEM) {
@@ -307,13 +280,15 @@ __global__ void __launch_bounds__(ColX2Geom<N>::THREADS, 1)
     float2* tb = tiles + b * G::TILE;
     const int next = tile + gridDim.x;
     auto prefetch_next = [&]() {
-      if (threadIdx.x == 0 && next < ntiles) {
-        bulk_wait_read<G::NB - 2>();
-        const int bn = (i + 1) % G::NB;
-        mbar_arrive_expect(&bars[bn], TILE_BYTES);
-        for (int kb = 0; kb < N / G::BH; ++kb)
-          tma_load_3d(tiles + bn * G::TILE + kb * G::BH * W, &map_in, (next % strips) * W, kb * G::BH,
-                      next / strips, &bars[bn]);
+      if constexpr (G::NB >= 2) {
+        if (threadIdx.x == 0 && next < ntiles) {
+          bulk_wait_read<G::NB - 2>();
+          const int bn = (i + 1) % G::NB;
+          mbar_arrive_expect(&bars[bn], TILE_BYTES);
+          for (int kb = 0; kb < N / G::BH; ++kb)
+            tma_load_3d(tiles + bn * G::TILE + kb * G::BH * W, &map_in, (next % strips) * W, kb * G::BH,
+                        next / strips, &bars[bn]);
+        }
       }
     };
     const int fb = tile / strips;  // field of the stack
@@ -380,6 +355,15 @@ __global__ void __launch_bounds__(ColX2Geom<N>::THREADS, 1)
       for (int kb = 0; kb < N / G::BH; ++kb)
         tma_store_3d(&map_out, (tile % strips) * W, kb * G::BH, fb, tb + kb * G::BH * W);
       bulk_commit();
+      if constexpr (G::NB == 1) {
+        // one buffer: the next strip lands in it once this store has read it out
+        if (next < ntiles) {
+          bulk_wait_read<0>();
+          mbar_arrive_expect(&bars[0], TILE_BYTES);
+          for (int kb = 0; kb < N / G::BH; ++kb)
+            tma_load_3d(tiles + kb * G::BH * W, &map_in, (next % strips) * W, kb * G::BH, next / strips, &bars[0]);
+        }
+      }
     }
   }
   if (threadIdx.x == 0) bulk_wait_all();
