@@ -78,6 +78,7 @@ _SIGS = {
                           _P, _P], c_int),
     "rs_detector_adjoint": ([_P, _P, _P, _P, ctypes.POINTER(DetectorGeom), _P], c_int),
     "rs_plan_set_pipeline": ([_P, c_int], c_int),
+    "rs_plan_set_cancel_flag": ([_P, ctypes.POINTER(c_int)], c_int),
     "rs_plan_set_schedule": ([_P, c_int], c_int),
     "rs_plan_is_four_step": ([_P], c_int),
     "rs_plan_get_schedule": ([_P, ctypes.POINTER(c_int)], c_int),
@@ -175,9 +176,18 @@ class Plan:
         with torch.cuda.device(self.device):
             check(lib().rs_plan_set_pipeline(self.handle, mask), "rs_plan_set_pipeline")
 
+    def set_cancel_flag(self, flag: "ctypes.c_int | None") -> None:
+        """Host flag the multislice loops read before each slice: non-zero stops the call with
+        InterruptedError (the field is then not a result). None turns the check off. The caller
+        keeps `flag` alive while it is set."""
+        self._cancel_flag = flag  # referenced here so the library never reads freed memory
+        check(lib().rs_plan_set_cancel_flag(self.handle, ctypes.byref(flag) if flag is not None else None),
+              "rs_plan_set_cancel_flag")
+
     def set_schedule(self, mask: int) -> None:
         """Pass schedule bits: 1 pipelined rows, 2 pipelined columns, 4 general row kernel,
-        8 split (three-pass) columns."""
+        8 split (three-pass) columns, 16 / 32 compensated rows / columns, 64 / 128 dithered
+        rows / columns one per thread group."""
         with torch.cuda.device(self.device):
             check(lib().rs_plan_set_schedule(self.handle, int(mask)), "rs_plan_set_schedule")
 

@@ -146,6 +146,8 @@ struct rs_plan {
   bool x2r_on = true, x2c_on = true;
   bool x2_rows = false, x2_cols = false;  // available for this plan's sizes
   bool d1_rows = true;                    // dithered rows one per thread group (RS_SCHED_SINGLE_ROWS)
+  bool d1_only_rows = false;              // dithered rows exist only one per thread group (no split pairs)
+  const volatile int* cancel = nullptr;   // host flag read between slices (rs_plan_set_cancel_flag)
   bool d1_cols = false;                   // dithered columns one per thread group (RS_SCHED_SINGLE_COLS)
   void* twd_arena = nullptr;
   float4* twd_x = nullptr;
@@ -566,7 +568,8 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
   // slice z's forward transform and slice z + 1's inverse use dithered table z mod K, so every
   // transform is undone by one with the same table.
   const bool plasma_rows_vox = !src.plasma || (p->fast && p->row_vox && !src.store);
-  const bool x2r = p->fast && p->x2r_on && p->x2_rows && plasma_rows_vox && g->nx_v <= row_x2_slots(p->nx);
+  const bool x2r = p->fast && p->x2r_on && (p->x2_rows || p->d1_only_rows) && plasma_rows_vox &&
+                   g->nx_v <= row_x2_slots(p->nx);
   auto table_x = [&](int z) { return p->twd_x + static_cast<size_t>(z % kDitherTables) * p->twd_x_len; };
   auto table1_x = [&](int z) { return p->twd1_x + static_cast<size_t>(z % kDitherTables) * p->twd_x_len; };
   // the dithered rows, as split pairs or one row per thread group (the same values)
@@ -581,10 +584,11 @@ int multislice(rs_plan* p, float2* u, float2* U, const SliceSource& src, const r
       r.twd1_inv = table1_x(z_inv);
       r.k_inv = p->kconst[z_inv % kDitherTables];
     }
-    return p->d1_rows ? launch_row_d1(p->nx, r, st) : launch_row_x2(p->nx, r, st);
+    return p->d1_rows || !p->x2_rows ? launch_row_d1(p->nx, r, st) : launch_row_x2(p->nx, r, st);
   };
   double cur_dz = NAN, cur_cs = NAN;
   for (int z = s0; z < s1; ++z) {
+    if (p->cancel && *p->cancel) return fail(RS_ECANCELLED, "cancelled before slice %d of [%d, %d)", z, s0, s1);
     const double dz = slice_dz[z];
     const double cs = coord_scale ? coord_scale[z] : 1.0;
     if (!(dz == cur_dz)) {
@@ -956,8 +960,9 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
   if (fast && (nx & (nx - 1)) == 0 && (ny & (ny - 1)) == 0) {
     int w = 0, bh = 0;
     p->x2_rows = row_x2_ok(nx);
+    p->d1_only_rows = !p->x2_rows && row_d1_only(nx);
     p->x2_cols = col_x2_box(ny, &w, &bh) && p->tw2_y != nullptr;
-    p->twd_x_len = p->x2_rows ? static_cast<int>(twx) : 0;
+    p->twd_x_len = p->x2_rows || p->d1_only_rows ? static_cast<int>(twx) : 0;
     p->twd_y2_len = p->x2_cols ? static_cast<int>(tw2y) : 0;
     const size_t n = static_cast<size_t>(p->twd_x_len + p->twd_y2_len) * kDitherTables;
     if (n > 0) {
@@ -968,7 +973,7 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
         p->twd_y2 = p->twd_x + static_cast<size_t>(p->twd_x_len) * kDitherTables;
         p->twd1_x = reinterpret_cast<float2*>(p->twd_x + n);
         p->twd1_y2 = p->twd1_x + static_cast<size_t>(p->twd_x_len) * kDitherTables;
-        if (p->x2_rows) e = launch_dither_tables(p->tws_x, p->twd_x, p->twd_x_len, 0);
+        if (p->twd_x_len > 0) e = launch_dither_tables(p->tws_x, p->twd_x, p->twd_x_len, 0);
         if (e == cudaSuccess && p->x2_cols) e = launch_dither_tables(p->tw2_y, p->twd_y2, p->twd_y2_len, 0);
         if (e == cudaSuccess) e = launch_single_tables(p->twd_x, p->twd1_x, n, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
@@ -1007,6 +1012,12 @@ int rs_plan_destroy(rs_plan* p) {
 int rs_plan_is_fast(const rs_plan* p) { return p && p->fast ? 1 : 0; }
 
 int rs_plan_is_four_step(const rs_plan* p) { return p && p->four ? 1 : 0; }
+
+int rs_plan_set_cancel_flag(rs_plan* p, const volatile int* flag) {
+  RS_TRY(check_plan(p));
+  p->cancel = flag;
+  return RS_OK;
+}
 
 int rs_plan_set_pipeline(rs_plan* p, int mask) {
   RS_TRY(check_plan(p));
@@ -1056,9 +1067,10 @@ int rs_plan_schedules(const rs_plan* p, int* masks, int cap, int* count) {
     if ((m & RS_SCHED_SINGLE_COLS) && ((m & RS_SCHED_COMP_COLS) || !p->x2_cols)) continue;
     // a direction without split-pair passes has only its single-sequence kernels; where the
     // split-pair passes run, the bits that choose among that direction's other kernels change nothing
-    if ((m & RS_SCHED_COMP_ROWS) && !p->x2_rows) continue;
+    if ((m & RS_SCHED_COMP_ROWS) && !p->x2_rows && !p->d1_only_rows) continue;
     if ((m & RS_SCHED_COMP_COLS) && !p->x2_cols) continue;
-    if (!(m & RS_SCHED_COMP_ROWS) && p->x2_rows && (m & (RS_SCHED_PIPE_ROWS | RS_SCHED_ROW_GENERAL))) continue;
+    if (!(m & RS_SCHED_COMP_ROWS) && (p->x2_rows || p->d1_only_rows) && (m & (RS_SCHED_PIPE_ROWS | RS_SCHED_ROW_GENERAL)))
+      continue;
     if (!(m & RS_SCHED_COMP_COLS) && p->x2_cols && (m & (RS_SCHED_PIPE_COLS | RS_SCHED_SPLIT_COLS))) continue;
     if ((m & RS_SCHED_SPLIT_COLS) && !p->split_ok) continue;
     if ((m & RS_SCHED_PIPE_ROWS) && !rows_pipe) continue;

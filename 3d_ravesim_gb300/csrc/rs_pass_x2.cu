@@ -96,10 +96,22 @@ cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const
 #define RS_D1ROW_CASE(N) \
   case N: return launch_rows_nvd<N, true, true>(a, s);
 
+// the dithered rows one per thread group also run at 16384, where a row pair does not fit shared
+// memory
+#define RS_D1_ONLY_ROW_SIZES(X) X(16384)
+
 cudaError_t launch_row_d1(int nx, const RowArgs& a, cudaStream_t s) {
   switch (nx) {
     RS_X2_ROW_SIZES(RS_D1ROW_CASE)
+    RS_D1_ONLY_ROW_SIZES(RS_D1ROW_CASE)
     default: return cudaErrorInvalidValue;
+  }
+}
+
+bool row_d1_only(int nx) {
+  switch (nx) {
+    RS_D1_ONLY_ROW_SIZES(RS_X2OK_CASE)
+    default: return false;
   }
 }
 

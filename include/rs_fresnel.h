@@ -246,6 +246,15 @@ typedef struct rs_detector_geom {
 int rs_detector(rs_plan* plan, const void* u, double* out, const rs_detector_geom* g,
                 void* stream);
 
+/* Cancellation of the multislice loops (rs_multislice_voxel, _stacked, _plasma, _dbgrid and its
+ * store / fields forms): with a flag set, each loop reads *flag (host memory, written by any host
+ * thread) before it enqueues a slice's passes and, when it is non-zero, returns RS_ECANCELLED
+ * (Python: InterruptedError) without enqueueing more. The passes already enqueued still run; the
+ * field is then part-way through the element and not a result. NULL (the default) turns the
+ * check off. Reference counterpart: the cancel tokens big-wave's long-running steps poll on the
+ * host (big-wave/propagation.py:669-680, checkpoint.py:22-30). */
+int rs_plan_set_cancel_flag(rs_plan* plan, const volatile int* flag);
+
 /* Pass variants: bulk-copy staged, persistent versions of the fused passes. mask bit 0 selects
  * them for the row passes, bit 1 for the column passes (default: columns only). RS_PIPELINE in
  * the environment ("0", "1", "rows", "cols") overrides the default at plan creation. */
@@ -284,7 +293,8 @@ int rs_plan_set_pipeline(rs_plan* plan, int mask);
 /*   RS_SCHED_SINGLE_ROWS (without RS_SCHED_COMP_ROWS) the dithered row passes hold one row per
  *                        thread group instead of two, in the single-sequence form of the same
  *                        arithmetic: the same results (up to the sign of zero) with half the
- *                        registers per thread. */
+ *                        registers per thread. Rows of 16384 have only this form (a row pair
+ *                        does not fit shared memory), so there the bit changes nothing. */
 #define RS_SCHED_SINGLE_ROWS 64
 /*   RS_SCHED_SINGLE_COLS (without RS_SCHED_COMP_COLS) the same for the dithered column passes:
  *                        one column per thread group (the strips of the pipelined single-sequence

@@ -28,6 +28,7 @@ def test_schedule_lists(rs, cuda):
     assert lib.plan_for(2048, 2048, cuda).schedules() == [0, 16, 17, 20, 32, 34, 48, 49, 50, 51, 52, 54,
                                                           64, 96, 98, 128, 144, 145, 148, 192]  # no split
     assert lib.plan_for(8192, 64, cuda).schedules() == [0, 16, 17, 20, 64]  # split-pair rows, 64-point columns
+    assert lib.plan_for(16384, 64, cuda).schedules() == [0, 16, 20]  # dithered rows only one per thread group
     assert lib.plan_for(72, 40, cuda).schedules() == [0]  # direct-DFT sizes have one schedule
     p = lib.plan_for(1024, 1024, cuda)
     old = p.schedule()

@@ -102,3 +102,33 @@ def test_run_allocates_nothing_after_setup(rs, cuda):
     second = run()
     assert rs._lib.alloc_count() == before
     np.testing.assert_array_equal(first[0], second[0])
+
+
+def test_cancel_flag_stops_the_multislice_loop(rs, cuda):
+    """A set cancel flag stops rs_multislice_voxel before its first slice with InterruptedError;
+    cleared, the same call runs to the field of an uncancelled plan."""
+    n = 256
+    dx = 0.5e-6
+    p = rs.SimParams(N=n * n, nx=n, ny=n, dx=dx, dy=dx, z_detector=1.0, detector_size=n * dx,
+                     detector_pixel_size_x=dx, detector_pixel_size_y=dx,
+                     wl=rs.convert_energy_wavelength(20000.0), chunk_size=n)
+    grid = np.random.default_rng(5).integers(0, 2, size=(4, n // 2 + 4, n // 2 + 4)).astype(np.uint32)
+    s = rs.Sample(z_start=0.5, pixel_size_x=2 * dx, pixel_size_z=1e-6, grid=grid,
+                  materials=[rs.Material("a", 1.0)], x_positions=np.array([0.0]), pixel_size_y=2 * dx,
+                  y_positions=np.array([0.0]))
+    s.db_list = np.array([0, 2e-7 + 1e-10j])
+    plan = rs._lib.plan_for(n, n, cuda)
+    flag = ctypes.c_int(1)
+    plan.set_cancel_flag(flag)
+    try:
+        u, U = rs.GpuVector.ones(n * n, cuda), rs.GpuVector.zeros(n * n, cuda)
+        with pytest.raises(InterruptedError, match="cancelled before slice 0"):
+            s.apply(u, U, p, 0.45 / dx, 0, None)
+        flag.value = 0
+        s.apply(u, U, p, 0.45 / dx, 0, None)
+        got = u.to_numpy()
+    finally:
+        plan.set_cancel_flag(None)
+    u2, U2 = rs.GpuVector.ones(n * n, cuda), rs.GpuVector.zeros(n * n, cuda)
+    s.apply(u2, U2, p, 0.45 / dx, 0, None)
+    np.testing.assert_array_equal(got, u2.to_numpy())
