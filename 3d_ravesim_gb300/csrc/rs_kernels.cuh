@@ -455,8 +455,9 @@ struct RowGeom {
   static constexpr size_t SMEM = PF ? BUF + static_cast<size_t>(ROWS) * PF_WORDS * 4 : BUF;
 };
 
-// VOX = true: the multislice hot path only (optional row IFFT, voxel transmission, row FFT, the
-// optional field store and scale), so the point-source and plasma code is not in the kernel.
+// VOX = true: the multislice hot path and plain row transforms only (optional row IFFT, optional
+// voxel transmission, row FFT, the optional field store and scale), so the point-source and
+// plasma code is not in the kernel.
 // DITH = true (with VOX, powers of two): the transforms use the slice's dithered tables
 // (twd1_inv / twd1_fwd, k_inv / k_fwd) in the single-sequence form of the split-pair arithmetic,
 // and the transmission is applied as the split-pair row kernel applies it, so the result is that
@@ -480,7 +481,7 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   float2 v[E];
 
   // Transmission row coordinates, and the prefetch of its two voxel rows (block-uniform decision).
-  const bool tmode = (VOX && !DITH) || (flags & (ROW_TVOX | ROW_TPLASMA));  // DITH: also the plain inverse
+  const bool tmode = (flags & (ROW_TVOX | ROW_TPLASMA)) != 0;  // VOX: also plain transforms
   const bool vox = VOX || (flags & ROW_TVOX);
   int yi = -1;
   float fy = 0.0f;

@@ -48,13 +48,15 @@ cudaError_t launch_rows_nv(const RowArgs& a, cudaStream_t s) {
   return launch_rows_nvd<N, VOX, false>(a, s);
 }
 
-// The voxel-transmission specialisation takes the multislice hot path (flags within
-// INV | FWD | TVOX | STORE_U | SCALE, TVOX set) unless the caller's schedule turns it off
-// (vox = false); every other combination runs the general kernel.
+// The voxel-transmission specialisation takes the multislice hot path and the plain row
+// transforms (flags within INV | FWD | TVOX | STORE_U | SCALE) unless the caller's schedule turns
+// it off for the multislice rows (vox = false, TVOX set); the point source (SRC) and the in-row
+// plasma transmission (TPLASMA) run the general kernel.
 template <int N>
 cudaError_t launch_rows_n(const RowArgs& a, bool vox, cudaStream_t s) {
   constexpr int HOT = ROW_INV | ROW_FWD | ROW_TVOX | ROW_STORE_U | ROW_SCALE;
-  if (RS_ROW_VOXMODE && vox && (a.flags & ROW_TVOX) && !(a.flags & ~HOT)) return launch_rows_nv<N, true>(a, s);
+  const bool hot = !(a.flags & ~HOT) && (vox || !(a.flags & ROW_TVOX));
+  if (RS_ROW_VOXMODE && hot) return launch_rows_nv<N, true>(a, s);
   return launch_rows_nv<N, false>(a, s);
 }
 
