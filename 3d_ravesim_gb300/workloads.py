@@ -20,8 +20,8 @@ import numpy as np
 from .optical_element import Material, Sample
 from .propagation import SimParams, convert_energy_wavelength
 
-# delta, beta of Si (2.33 g/cm^3) at 25 keV from the Chantler tables (nist_lookup's method,
-# restated by tests/golden/chantler_constants.py).
+# delta, beta of Si (2.33 g/cm^3) at 25 keV from the Chantler tables (`chantler.xray_delta_beta`
+# over nist_lookup's database), kept as numbers so the workload needs no database.
 SI_DELTA_BETA_25KEV = (7.734971368200993e-07, 2.1375609561035094e-09)
 
 
