@@ -10,7 +10,11 @@ its parsing of a prepared directory, and its own setup_simulation file by file:
 * setup_ref_fresnel/: 256 x 256 with use_fresnel_scaling and one voxel sample, the detector
   larger than the grid (the similarity frame), four sources;
 * setup_ref_exit/: a voxel sample followed by a save_and_exit marker and a second sample (the
-  element list cut at the marker, the detector moved to it), two sources.
+  element list cut at the marker, the detector moved to it), two sources;
+* setup_errors.json: the exception type and message big-wave raises for each input of
+  `setup_cases.error_cases` (non-power-of-two axis, detector larger than the grid, the source-to-sample
+  and the cutoff Nyquist conditions, reflections at the boundary, thin Fresnel scaling with two elements, an unknown
+  multisource, a bad y_range, overlapping elements, a non-integer chunk size).
 
 big-wave needs two things this container does not have, which the script supplies:
 * ruamel.yaml: config.load / config.save go through a stand-in backed by this package's
@@ -30,6 +34,7 @@ fourth row and column of the field it saved.
 from __future__ import annotations
 
 import importlib
+import json
 import shutil
 import sys
 import tempfile
@@ -40,7 +45,7 @@ sys.path.insert(0, str(HERE))
 sys.path.insert(0, str(HERE.parents[1]))
 from make_chantler_golden import _fake_sqlalchemy  # noqa: E402
 from make_golden import import_reference  # noqa: E402
-from setup_cases import CASES, RUN_CASES, write_inputs  # noqa: E402
+from setup_cases import CASES, RUN_CASES, error_cases, write_inputs  # noqa: E402
 
 import numpy as np  # noqa: E402
 
@@ -88,8 +93,19 @@ def main(root: Path) -> None:
                 if u_file.exists():
                     n = CASES[name]()["sim_params"]
                     runs[f"{name}_u_sub"] = np.load(u_file).reshape(n["ny"], n["nx"])[::4, ::4].copy()
+        # the inputs big-wave rejects: the exception type and message of each
+        errors = {}
+        for name, dct in error_cases().items():
+            try:
+                ms.setup_simulation(dct, tmp, tmp / f"err_{name}")
+            except Exception as exc:  # noqa: BLE001 - every rejection is recorded as raised
+                errors[name] = [type(exc).__name__, str(exc)]
+            else:
+                raise SystemExit(f"big-wave accepted the error case {name}")
     np.savez(HERE / "setup_runs.npz", **runs)
     print("wrote", HERE / "setup_runs.npz", sorted(runs))
+    (HERE / "setup_errors.json").write_text(json.dumps(errors, indent=1) + "\n")
+    print("wrote", HERE / "setup_errors.json")
 
 
 if __name__ == "__main__":

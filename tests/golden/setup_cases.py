@@ -102,3 +102,39 @@ def write_inputs(tmp: Path) -> None:
 
 # cases whose source 0 big-wave also runs (tests/golden/setup_runs.npz)
 RUN_CASES = ("setup_ref_plasma", "setup_ref_fresnel", "setup_ref_exit")
+
+
+def _with(base: dict, **changes) -> dict:
+    """A copy of `base` with top-level keys, or sim_params / multisource entries ("sp_x", "ms_x"),
+    replaced."""
+    import copy
+    out = copy.deepcopy(base)
+    for key, value in changes.items():
+        if key.startswith("sp_"):
+            out["sim_params"][key[3:]] = value
+        elif key.startswith("ms_"):
+            out["multisource"][key[3:]] = value
+        else:
+            out[key] = value
+    return out
+
+
+def error_cases() -> dict:
+    """Inputs big-wave's setup_simulation rejects, each with the exception it raises (recorded in
+    tests/golden/setup_errors.json)."""
+    base = config_dict()
+    return {
+        "nx_not_power_of_two": _with(base, sp_N=384 * 256, sp_nx=384),
+        "detector_bigger_than_grid": _with(base, sp_detector_size=1e-4, sp_detector_size_x=1e-4),
+        "source_nyquist_exceeded": _with(base, sp_dx=4e-7, sp_dy=4e-7, sp_z_detector=0.5 + 6e-6,
+                                         elements=[_sample(0.5, "grid.npy")]),
+        "reflections_at_boundary": _with(base, ms_x_range=[-4e-6, 4e-6], sp_detector_size=2.56e-5,
+                                         sp_detector_size_x=2.56e-5, sp_detector_size_y=2.56e-5),
+        "thin_fresnel_two_elements": _with(config_fresnel(), elements=[_sample(0.5, "grid.npy"),
+                                                                       _sample(0.6, "grid2.npy", (["Au", 19.32],))]),
+        "cutoff_beyond_nyquist": _with(base, sp_z_detector=0.5 + 1.4e-5),
+        "unknown_multisource": _with(base, ms_type="cloud"),
+        "y_range_not_a_pair": _with(base, ms_y_range=[0.0]),
+        "overlapping_elements": _with(base, elements=[_sample(0.5, "grid.npy"), _sample(0.5 + 1e-6, "grid2.npy")]),
+        "bad_chunk_size": _with(base, sp_chunk_size=1.5),
+    }

@@ -8,7 +8,9 @@ The delta/beta tables and plasma scattering factors come from the Chantler datab
 nist_lookup's xrayref.db is not found, the lookups are answered from the fixture's own values
 (the Chantler arithmetic is pinned bit for bit by test_chantler_host.py), so everything else of
 the setup is still checked."""
+import builtins
 import importlib
+import json
 import sys
 from pathlib import Path
 
@@ -147,3 +149,19 @@ def test_resolve_sim_params_rules(mods):
                       "P0 memory gate")):
         with pytest.raises(ValueError, match=msg):
             cfg.resolve_sim_params({**base, **bad})
+
+
+ERRORS = json.loads((GOLDEN / "setup_errors.json").read_text())
+
+
+@pytest.mark.parametrize("name", sorted(ERRORS))
+def test_setup_simulation_rejects_like_bigwave(mods, chantler_answers, tmp_path, name):
+    """The inputs big-wave's setup_simulation rejects raise the same exception type and message
+    here, and leave no simulation directory behind."""
+    from setup_cases import error_cases
+    kind, message = ERRORS[name]
+    chantler_answers(GOLDEN / "setup_ref")
+    with pytest.raises(getattr(builtins, kind)) as exc:  # setup_ref_exit/ holds both grids
+        mods["prepare"].setup_simulation(error_cases()[name], GOLDEN / "setup_ref_exit", tmp_path / "out")
+    assert str(exc.value) == message
+    assert not (tmp_path / "out").exists()
