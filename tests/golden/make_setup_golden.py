@@ -14,7 +14,9 @@ its parsing of a prepared directory, and its own setup_simulation file by file:
 * setup_errors.json: the exception type and message big-wave raises for each input of
   `setup_cases.error_cases` (non-power-of-two axis, detector larger than the grid, the source-to-sample
   and the cutoff Nyquist conditions, reflections at the boundary, thin Fresnel scaling with two elements, an unknown
-  multisource, a bad y_range, overlapping elements, a non-integer chunk size).
+  multisource, a bad y_range, overlapping elements, a non-integer chunk size);
+* setup_rules.json: big-wave's compute_cutoff_angles on 60 seeded geometries and its
+  resolve_sim_params on 40 seeded requests, with their outputs or exceptions.
 
 big-wave needs two things this container does not have, which the script supplies:
 * ruamel.yaml: config.load / config.save go through a stand-in backed by this package's
@@ -106,6 +108,58 @@ def main(root: Path) -> None:
     print("wrote", HERE / "setup_runs.npz", sorted(runs))
     (HERE / "setup_errors.json").write_text(json.dumps(errors, indent=1) + "\n")
     print("wrote", HERE / "setup_errors.json")
+    (HERE / "setup_rules.json").write_text(json.dumps(rule_cases(_prop, bw_config), indent=1) + "\n")
+    print("wrote", HERE / "setup_rules.json")
+
+
+def rule_cases(prop, bw_config) -> dict:
+    """big-wave's compute_cutoff_angles (propagation.py:524-622) on seeded geometries, and its
+    resolve_sim_params (config.py:230-315) on seeded sim_params / runtime requests: the inputs
+    with the outputs, or the exception each raises."""
+    rng = np.random.default_rng(11)
+    cutoffs = []
+    for i in range(60):
+        n_el = int(rng.integers(0, 4))
+        z_det = float(rng.uniform(0.5, 3.0))
+        zs = sorted(float(v) for v in rng.uniform(0.05, z_det * 0.9, n_el))
+        heights = [float(v) for v in rng.uniform(1e-6, 2e-3, n_el)]
+        if n_el and i % 5 == 0:  # the detector right behind the last element
+            z_det = zs[-1] + heights[-1] + float(rng.uniform(0, 5e-9))
+        args = {"detector_size": float(rng.uniform(1e-5, 5e-3)), "dx": float(10 ** rng.uniform(-8.5, -7)),
+                "energy_range": sorted(float(v) for v in rng.uniform(5e3, 5e4, 2)), "z_source": 0.0,
+                "z_distances": zs, "element_heights": heights, "z_detector": z_det,
+                "max_x": float(rng.uniform(0, 2e-4))}
+        try:
+            angles, widths = prop.compute_cutoff_angles(**{**args, "energy_range": tuple(args["energy_range"])})
+            cutoffs.append({"args": args, "angles": [float(a) for a in angles], "widths": [float(w) for w in widths]})
+        except Exception as exc:  # noqa: BLE001
+            cutoffs.append({"args": args, "error": [type(exc).__name__, str(exc)]})
+    resolves = []
+    for i in range(40):
+        ny = int(2 ** rng.integers(1, 12))
+        nx = int(2 ** rng.integers(4, 14))
+        sim = {"N": nx * ny, "ny": ny, "dx": 1e-7, "z_detector": 1.0, "detector_pixel_size_x": 1e-6,
+               "detector_pixel_size_y": 1e-6}
+        if i % 3:
+            sim["nx"] = nx
+        runtime = {}
+        choice = int(rng.integers(0, 4))
+        if choice == 0:
+            sim["chunk_size"] = int(rng.integers(1, nx * ny * 2))
+        elif choice == 1:
+            runtime["chunk_size"] = "auto"
+        if i % 4 == 0:
+            runtime["memory_budget_gb"] = float(rng.choice([0.25, 0.5, 1.0, 2.0, 6.0, 64.0]))
+        if i % 7 == 0:
+            runtime["detector_integrator"] = "legacy_fastwave"
+        dct = {"sim_params": sim, "dtype": str(rng.choice(["c8", "c16"]))}
+        if runtime:
+            dct["runtime"] = {"big_wave": runtime}
+        try:
+            resolves.append({"dct": dct, "out": bw_config.resolve_sim_params(dct)})
+        except Exception as exc:  # noqa: BLE001
+            resolves.append({"dct": dct, "error": [type(exc).__name__, str(exc)]})
+    return {"compute_cutoff_angles": cutoffs, "resolve_sim_params": resolves}
 
 
 if __name__ == "__main__":

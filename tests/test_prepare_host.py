@@ -165,3 +165,35 @@ def test_setup_simulation_rejects_like_bigwave(mods, chantler_answers, tmp_path,
         mods["prepare"].setup_simulation(error_cases()[name], GOLDEN / "setup_ref_exit", tmp_path / "out")
     assert str(exc.value) == message
     assert not (tmp_path / "out").exists()
+
+
+RULES = json.loads((GOLDEN / "setup_rules.json").read_text())
+
+
+def test_compute_cutoff_angles_matches_bigwave_bit_for_bit(mods):
+    """60 seeded geometries (0-3 elements, the detector right behind the last element in some)
+    through big-wave's compute_cutoff_angles and this package's: the same angles and beam
+    half-widths to the last bit, or the same exception."""
+    prop = mods["propagation"]
+    for case in RULES["compute_cutoff_angles"]:
+        args = {**case["args"], "energy_range": tuple(case["args"]["energy_range"])}
+        if "error" in case:
+            with pytest.raises(getattr(builtins, case["error"][0])) as exc:
+                prop.compute_cutoff_angles(**args)
+            assert str(exc.value) == case["error"][1]
+            continue
+        angles, widths = prop.compute_cutoff_angles(**args)
+        assert angles == case["angles"] and widths == case["widths"], case["args"]
+
+
+def test_resolve_sim_params_matches_bigwave(mods):
+    """40 seeded sim_params / runtime requests (explicit and auto chunk sizes, budgets, dtypes)
+    resolved as big-wave resolves them, or rejected with its message."""
+    cfg = mods["config"]
+    for case in RULES["resolve_sim_params"]:
+        if "error" in case:
+            with pytest.raises(getattr(builtins, case["error"][0])) as exc:
+                cfg.resolve_sim_params(case["dct"])
+            assert str(exc.value) == case["error"][1]
+            continue
+        assert cfg.resolve_sim_params(case["dct"]) == case["out"], case["dct"]
