@@ -1528,7 +1528,17 @@ int rs_adjoint_multislice_dbgrid_ex(rs_plan* p, void* g, const float* db_grid, c
     r.vox.a = a;
     r.aux = const_cast<float2*>(static_cast<const float2*>(fields)) + static_cast<size_t>(z - slice_begin) * n;
     r.grad = grad_grid + plane * z * 2;
-    RS_CK(launch_row_adjoint(p->nx, r, s));
+    if (p->x2r_on && (p->x2_rows || p->d1_only_rows)) {
+      // dithered tables: slice z's inverse undoes slice z + 1's forward, both with table z + 1
+      const int ti = (z + 1) % kDitherTables, tf = z % kDitherTables;
+      r.twd1_inv = p->twd1_x + static_cast<size_t>(ti) * p->twd_x_len;
+      r.twd1_fwd = p->twd1_x + static_cast<size_t>(tf) * p->twd_x_len;
+      r.k_inv = p->kconst[ti];
+      r.k_fwd = p->kconst[tf];
+      RS_CK(launch_row_adjoint_d1(p->nx, r, s));
+    } else {
+      RS_CK(launch_row_adjoint(p->nx, r, s));
+    }
   }
   return RS_OK;
 }

@@ -634,7 +634,9 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
 // added up per voxel, and each block adds its sums to the grid with one global atomic per touched
 // value. The y weights (1 - fy, fy) are the same for every pixel of the row, so they are applied
 // once per voxel.
-template <int N, int ROWS>
+// DITH: the row transforms use dithered tables (twd1_inv / twd1_fwd, k_inv / k_fwd) in the
+// single-sequence form, as the default multislice row pass does.
+template <int N, int ROWS, bool DITH = false>
 __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row_adjoint_kernel(const RowArgs a) {
   using P = FftPlan<N>;
   constexpr int T = P::T;
@@ -661,7 +663,11 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   if (flags & ROW_INV) {
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = valid ? a.in[rbase + slot_pos<N, RX>(t, e)] : make_float2(0.f, 0.f);
-    fft_seq<N, true>(v, buf, t, a.tw);
+    if constexpr (DITH) {
+      fft_seq2x<N, true>(v, buf, t, a.twd1_inv, dft_k1(a.k_inv));
+    } else {
+      fft_seq<N, true>(v, buf, t, a.tw);
+    }
   } else {
 #pragma unroll
     for (int e = 0; e < E; ++e) v[e] = valid ? a.in[rbase + slot_pos<N, RF>(t, e)] : make_float2(0.f, 0.f);
@@ -678,26 +684,41 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   if (yi >= 0) {
     const float k = 12.566370614359172f * a.vox.a;  // 4 pi t / wl
     float* mine = acc + (threadIdx.x % copies) * stride;
+    // two pixels at a time: their factors in packed arithmetic (each pixel's bits are those
+    // material_factor gives it), then each pixel's gradient and conj(t) v
 #pragma unroll
-    for (int e = 0; e < E; ++e) {
-      const int x = slot_pos<N, RF>(t, e);
-      const int2 xe = __ldg(&a.ax.xp[x]);
-      const int xi = xe.x;
-      if (xi < 0) continue;  // outside the grid: t = 1 and no voxel depends on this pixel
-      const float fx = __int_as_float(xe.y);
-      const float2 d = lerp2(buf[xi], buf[xi + 1], fx);
-      const float2 tr = material_factor(d.x, d.y, a.vox.a);
-      const float2 uu = a.aux[rbase + x];
-      const float2 G = cmulc(v[e], uu);   // conj(u) v
-      const float2 q = cmulc(tr, G);      // t conj(G)
-      const float gd = k * q.y, gb = -k * q.x;
-      const float gx0 = 1.0f - fx;
-      float* r0 = mine + 2 * xi;
-      atomicAdd(r0, gx0 * gd);
-      atomicAdd(r0 + 1, gx0 * gb);
-      atomicAdd(r0 + 2, fx * gd);
-      atomicAdd(r0 + 3, fx * gb);
-      v[e] = cmulc(v[e], tr);               // conj(t) v
+    for (int e0 = 0; e0 < E; e0 += 2) {
+      int xs[2], xis[2];
+      float fxs[2];
+      float2 ds[2];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        xs[h] = slot_pos<N, RF>(t, e0 + h);
+        const int2 xe = __ldg(&a.ax.xp[xs[h]]);
+        xis[h] = xe.x;
+        fxs[h] = __int_as_float(xe.y);
+        ds[h] = xis[h] >= 0 ? lerp2(buf[xis[h]], buf[xis[h] + 1], fxs[h]) : make_float2(0.f, 0.f);
+      }
+      const cp2 trs = material_factor2(ds[0], ds[1], a.vox.a);
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int xi = xis[h];
+        if (xi < 0) continue;  // outside the grid: t = 1 and no voxel depends on this pixel
+        const int e = e0 + h;
+        const float fx = fxs[h];
+        const float2 tr = h == 0 ? make_float2(trs.re.x, trs.im.x) : make_float2(trs.re.y, trs.im.y);
+        const float2 uu = a.aux[rbase + xs[h]];
+        const float2 G = cmulc(v[e], uu);   // conj(u) v
+        const float2 q = cmulc(tr, G);      // t conj(G)
+        const float gd = k * q.y, gb = -k * q.x;
+        const float gx0 = 1.0f - fx;
+        float* r0 = mine + 2 * xi;
+        atomicAdd(r0, gx0 * gd);
+        atomicAdd(r0 + 1, gx0 * gb);
+        atomicAdd(r0 + 2, fx * gd);
+        atomicAdd(r0 + 3, fx * gb);
+        v[e] = cmulc(v[e], tr);               // conj(t) v
+      }
     }
   }
   __syncthreads();
@@ -715,7 +736,11 @@ __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row
   }
   __syncthreads();  // the forward transform reuses the buffer
   if (flags & ROW_FWD) {
-    fft_seq<N, false>(v, buf, t, a.tw);
+    if constexpr (DITH) {
+      fft_seq2x<N, false>(v, buf, t, a.twd1_fwd, dft_k1(a.k_fwd));
+    } else {
+      fft_seq<N, false>(v, buf, t, a.tw);
+    }
     if (valid) {
 #pragma unroll
       for (int e = 0; e < E; ++e) a.out[rbase + slot_pos<N, RX>(t, e)] = v[e];

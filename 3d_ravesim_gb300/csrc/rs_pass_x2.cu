@@ -108,6 +108,17 @@ cudaError_t launch_row_d1(int nx, const RowArgs& a, cudaStream_t s) {
   }
 }
 
+#define RS_D1ADJ_CASE(N) \
+  case N: return launch_row_adjoint_n<N, true>(a, s);
+
+cudaError_t launch_row_adjoint_d1(int nx, const RowArgs& a, cudaStream_t s) {
+  switch (nx) {
+    RS_X2_ROW_SIZES(RS_D1ADJ_CASE)
+    RS_D1_ONLY_ROW_SIZES(RS_D1ADJ_CASE)
+    default: return cudaErrorInvalidValue;
+  }
+}
+
 bool row_d1_only(int nx) {
   switch (nx) {
     RS_D1_ONLY_ROW_SIZES(RS_X2OK_CASE)

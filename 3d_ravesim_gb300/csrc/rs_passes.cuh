@@ -60,7 +60,7 @@ cudaError_t launch_rows_n(const RowArgs& a, bool vox, cudaStream_t s) {
   return launch_rows_nv<N, false>(a, s);
 }
 
-template <int N>
+template <int N, bool DITH = false>
 cudaError_t launch_row_adjoint_n(const RowArgs& a, cudaStream_t s) {
   constexpr int ROWS = rows_per_block<N>();
   constexpr int THREADS = ROWS * FftPlan<N>::T;
@@ -70,12 +70,12 @@ cudaError_t launch_row_adjoint_n(const RowArgs& a, cudaStream_t s) {
   if (cudaGetDevice(&dev) != cudaSuccess) return cudaErrorInvalidDevice;
   const unsigned bit = 1u << (dev & 31);
   if (!(configured & bit)) {
-    cudaError_t e = cudaFuncSetAttribute(row_adjoint_kernel<N, ROWS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(row_adjoint_kernel<N, ROWS, DITH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          static_cast<int>(SMEM));
     if (e != cudaSuccess) return e;
     configured |= bit;
   }
-  row_adjoint_kernel<N, ROWS><<<(a.ny + ROWS - 1) / ROWS, THREADS, SMEM, s>>>(a);
+  row_adjoint_kernel<N, ROWS, DITH><<<(a.ny + ROWS - 1) / ROWS, THREADS, SMEM, s>>>(a);
   const cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) note_launch();
   return e;

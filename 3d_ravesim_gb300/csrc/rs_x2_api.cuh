@@ -12,6 +12,8 @@ cudaError_t launch_row_x2(int nx, const RowArgs& a, cudaStream_t s);
 // the same row pass with one row per thread group (row_pass_kernel<N, ROWS, true, true>), for the
 // row_x2_ok sizes; reads twd1_inv / twd1_fwd
 cudaError_t launch_row_d1(int nx, const RowArgs& a, cudaStream_t s);
+// the adjoint row pass with the dithered tables (row_adjoint_kernel<N, ROWS, true>)
+cudaError_t launch_row_adjoint_d1(int nx, const RowArgs& a, cudaStream_t s);
 // sizes with dithered rows one per thread group but no split-pair rows (16384)
 bool row_d1_only(int nx);
 cudaError_t launch_col_x2(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
