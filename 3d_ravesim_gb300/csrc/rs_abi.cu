@@ -805,13 +805,15 @@ size_t det_layout(const DetTables& t, size_t o[8]) {
 
 }  // namespace
 
-// Dithered copies of cos(pi/8), sin(pi/8) and sqrt(2)/2 for the split-pair DFTs: in copy j each
+// Dithered copies of cos(pi/8), sin(pi/8), sqrt(2)/2 (radix 8 and 16) and cos(pi/12), sin(pi/12),
+// sqrt(3)/2 (radix 3 and 24) for the dithered DFTs: in copy j each
 // constant is one of the two floats bracketing its exact value, the upper one in a fraction of
 // the copies equal to the exact value's position between them (the rule of the twiddle tables).
 void dither_consts(DftConsts* k) {
-  const double exact[3] = {std::cos(M_PI / 8.0), std::sin(M_PI / 8.0), std::sqrt(0.5)};
-  float out[3][kDitherTables];
-  for (int c = 0; c < 3; ++c) {
+  const double exact[6] = {std::cos(M_PI / 8.0),  std::sin(M_PI / 8.0),  std::sqrt(0.5),
+                           std::cos(M_PI / 12.0), std::sin(M_PI / 12.0), std::sqrt(3.0) / 2.0};
+  float out[6][kDitherTables];
+  for (int c = 0; c < 6; ++c) {
     const float h = static_cast<float>(exact[c]);
     const double l = exact[c] - static_cast<double>(h);
     const float other = std::nextafter(h, l > 0 ? INFINITY : -INFINITY);
@@ -820,7 +822,8 @@ void dither_consts(DftConsts* k) {
     const int off = (17 * c + 5) % kDitherTables;
     for (int j = 0; j < kDitherTables; ++j) out[c][j] = ((j + off) % kDitherTables) < n_other ? other : h;
   }
-  for (int j = 0; j < kDitherTables; ++j) k[j] = DftConsts{out[0][j], out[1][j], out[2][j]};
+  for (int j = 0; j < kDitherTables; ++j)
+    k[j] = DftConsts{out[0][j], out[1][j], out[2][j], out[3][j], out[4][j], out[5][j]};
 }
 
 // ======================================================================== extern "C"
@@ -956,8 +959,9 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
     delete p;
     return fail(RS_ECUDA, "twiddle setup: %s", cudaGetErrorString(e));
   }
-  // split-pair multislice passes: dithered tables derived from the compensated ones
-  if (fast && (nx & (nx - 1)) == 0 && (ny & (ny - 1)) == 0) {
+  // dithered multislice passes: tables derived from the compensated ones (rows of 2^k and 3*2^k,
+  // split-pair columns of 2^k)
+  if (fast) {
     int w = 0, bh = 0;
     p->x2_rows = row_x2_ok(nx);
     p->d1_only_rows = !p->x2_rows && row_d1_only(nx);

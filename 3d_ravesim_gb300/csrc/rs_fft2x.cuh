@@ -26,6 +26,8 @@
 // each lane, in the same order, so a single-sequence transform gives the bits of the split-pair
 // one (up to the sign of zero) with half the registers per thread.
 #pragma once
+#include <type_traits>
+
 #include "rs_fft.cuh"
 
 namespace rs {
@@ -82,6 +84,7 @@ __device__ __forceinline__ cp2 x_mul_tw(cp2 a, float2 w) {
 // sqrt(2)/2, each dithered like the twiddle tables (host-built, one set per table).
 struct DftConsts {
   float c8, s8, r2;
+  float c12, s12, h3;  // cos(pi/12), sin(pi/12), sqrt(3)/2: the radix-24 / radix-3 constants
 };
 struct DftK {
   float2 c8, nc8, s8, ns8, r2, nr2;
@@ -93,9 +96,9 @@ __device__ __forceinline__ DftK dft_k(const DftConsts& k) {
 
 // ---- single-sequence form: the lane operations above on one (re, im) value
 struct DftK1 {
-  float c8, s8, r2;
+  float c8, s8, r2, c12, s12, h3;
 };
-__device__ __forceinline__ DftK1 dft_k1(const DftConsts& k) { return {k.c8, k.s8, k.r2}; }
+__device__ __forceinline__ DftK1 dft_k1(const DftConsts& k) { return {k.c8, k.s8, k.r2, k.c12, k.s12, k.h3}; }
 
 __device__ __forceinline__ float2 x_add(float2 a, float2 b) { return p_add(a, b); }
 __device__ __forceinline__ float2 x_sub(float2 a, float2 b) { return p_sub(a, b); }
@@ -137,6 +140,76 @@ __device__ __forceinline__ float2 tw16x(float2 a, const DftK1& k) {
     static_assert(M == 9, "W16 power");
     return INV ? x_mul3(a, -k.c8, -k.s8, k.s8) : x_mul3(a, -k.c8, k.s8, -k.s8);
   }
+}
+
+// 3-point DFT (as dft3 of rs_common.cuh) with the slice's dithered sqrt(3)/2:
+// y0 = a0 + t, y1,2 = a0 - t/2 -+ i h3 (a1 - a2) (forward), t = a1 + a2.
+template <bool INV>
+__device__ __forceinline__ void dft3x(float2& a0, float2& a1, float2& a2, const DftK1& k) {
+  const float2 t = x_add(a1, a2);
+  const float2 d = x_sub(a1, a2);
+  const float2 m = make_float2(fmaf(-0.5f, t.x, a0.x), fmaf(-0.5f, t.y, a0.y));
+  const float2 q = INV ? make_float2(-d.y * k.h3, d.x * k.h3) : make_float2(d.y * k.h3, -d.x * k.h3);
+  a0 = x_add(a0, t);
+  a1 = x_add(m, q);
+  a2 = x_sub(m, q);
+}
+
+// Multiply by W24^M = exp(-+2 pi i M/24) for the M used inside the 3 x 8 radix-24 butterfly,
+// with the slice's dithered constants (the halves are exact).
+template <int M, bool INV>
+__device__ __forceinline__ float2 tw24x(float2 a, const DftK1& k) {
+  if constexpr (M == 0) {
+    return a;
+  } else if constexpr (M == 3) {
+    return tw16x<2, INV>(a, k);  // 45 degrees
+  } else if constexpr (M == 6) {
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+  } else if constexpr (M == 12) {
+    return make_float2(-a.x, -a.y);
+  } else {
+    static_assert(M == 1 || M == 2 || M == 4 || M == 5 || M == 7 || M == 8 || M == 10 || M == 14, "W24 power");
+    // forward exp(-i 15 deg M) = (wr, wi)
+    const float wr = M == 1 ? k.c12 : M == 2 ? k.h3 : M == 4 ? 0.5f : M == 5 ? k.s12 : M == 7 ? -k.s12
+                   : M == 8 ? -0.5f : -k.h3;                                           // M = 10, 14
+    const float wi0 = M == 1 ? -k.s12 : M == 2 ? -0.5f : M == 4 ? -k.h3 : M == 5 ? -k.c12
+                    : M == 7 ? -k.c12 : M == 8 ? -k.h3 : M == 10 ? -0.5f : 0.5f;       // M = 14
+    const float wi = INV ? -wi0 : wi0;
+    return x_mul3(a, wr, wi, -wi);
+  }
+}
+
+template <int K1, bool INV, int... N2>
+__device__ __forceinline__ void tw24x_row(float2 (&a)[24], const DftK1& k, std::integer_sequence<int, N2...>) {
+  ((a[8 * K1 + N2] = tw24x<N2 * K1, INV>(a[8 * K1 + N2], k)), ...);
+}
+
+template <bool INV, class V, class K>
+__device__ __forceinline__ void dft8x(V (&a)[8], const K& k);  // below
+
+// 24-point DFT as 3 x 8 (as dft24 of rs_common.cuh), natural order in and out.
+template <bool INV>
+__device__ __forceinline__ void dft24x(float2 (&a)[24], const DftK1& k) {
+#pragma unroll
+  for (int n2 = 0; n2 < 8; ++n2) dft3x<INV>(a[n2], a[8 + n2], a[16 + n2], k);
+  tw24x_row<1, INV>(a, k, std::make_integer_sequence<int, 8>{});
+  tw24x_row<2, INV>(a, k, std::make_integer_sequence<int, 8>{});
+#pragma unroll
+  for (int k1 = 0; k1 < 3; ++k1) {
+    float2 b[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) b[i] = a[8 * k1 + i];
+    dft8x<INV>(b, k);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[8 * k1 + i] = b[i];
+  }
+  float2 y[24];
+#pragma unroll
+  for (int k1 = 0; k1 < 3; ++k1)
+#pragma unroll
+    for (int k2 = 0; k2 < 8; ++k2) y[k1 + 3 * k2] = a[8 * k1 + k2];
+#pragma unroll
+  for (int i = 0; i < 24; ++i) a[i] = y[i];
 }
 
 // Value type -> its twiddle-table entry and DFT-constant types.
@@ -243,10 +316,13 @@ __device__ __forceinline__ void dft16x(V (&a)[16], const K& k) {
   for (int i = 0; i < 16; ++i) a[i] = y[i];
 }
 
-template <int R, bool INV, int OFF, class V, class K>
-__device__ __forceinline__ void dft_slice2x(V (&v)[16], const K& k) {
-  if constexpr (R == 16) {
-    static_assert(OFF == 0, "radix-16 stages use the whole array");
+template <int R, bool INV, int OFF, class V, class K, int E>
+__device__ __forceinline__ void dft_slice2x(V (&v)[E], const K& k) {
+  if constexpr (R == 24) {
+    static_assert(OFF == 0 && E == 24, "radix-24 stages use the whole array");
+    dft24x<INV>(v, k);
+  } else if constexpr (R == 16) {
+    static_assert(OFF == 0 && E == 16, "radix-16 stages use the whole array");
     dft16x<INV>(v, k);
   } else if constexpr (R == 8) {
     V a[8];
@@ -262,8 +338,8 @@ __device__ __forceinline__ void dft_slice2x(V (&v)[16], const K& k) {
   }
 }
 
-template <int R, bool INV, class V, class K, int... Bs>
-__device__ __forceinline__ void dft_all2x(V (&v)[16], const K& k, std::integer_sequence<int, Bs...>) {
+template <int R, bool INV, class V, class K, int E, int... Bs>
+__device__ __forceinline__ void dft_all2x(V (&v)[E], const K& k, std::integer_sequence<int, Bs...>) {
   (dft_slice2x<R, INV, Bs * R>(v, k), ...);
 }
 
@@ -277,10 +353,11 @@ struct FftStages2x {
   using P = FftPlan<N>;
   using Tw = TwT;
   using K = typename XForm<V>::K;
-  static_assert(P::POW2, "split-pair transforms are built for power-of-two lengths");
-  static __device__ __forceinline__ void run(V (&v)[16], V* buf, int t, const Tw* __restrict__ tw, const K& k) {
+  static constexpr int E = P::E;
+  static_assert(P::POW2 || std::is_same<V, float2>::value, "split pairs are built for power-of-two lengths");
+  static __device__ __forceinline__ void run(V (&v)[E], V* buf, int t, const Tw* __restrict__ tw, const K& k) {
     constexpr int R = P::radix(INV, SI);
-    constexpr int B = 16 / R;
+    constexpr int B = E / R;
     constexpr int T = P::T;
     if constexpr (NS > 1) {
 #pragma unroll
@@ -307,7 +384,7 @@ struct FftStages2x {
       if constexpr (WARP) __syncwarp(); else __syncthreads();
       const int pt = AD::at(t);
 #pragma unroll
-      for (int e = 0; e < 16; ++e) v[e] = buf[AD::at_plus(t, pt, slot_pos<N, R2>(0, e), false) * STR];
+      for (int e = 0; e < E; ++e) v[e] = buf[AD::at_plus(t, pt, slot_pos<N, R2>(0, e), false) * STR];
       if constexpr (!WARP) __syncthreads();
       FftStages2x<N, INV, SI + 1, NS * R, AD, WARP, TWL, STR, V, TwT>::run(v, buf, t, tw, k);
     }
@@ -315,7 +392,8 @@ struct FftStages2x {
 };
 
 template <int N, bool INV, class AD = PadAddr, class TWL = TwGlobal, class V>
-__device__ __forceinline__ void fft_seq2x(V (&v)[16], V* buf, int t, const typename XForm<V>::Tw* __restrict__ tw,
+__device__ __forceinline__ void fft_seq2x(V (&v)[FftPlan<N>::E], V* buf, int t,
+                                          const typename XForm<V>::Tw* __restrict__ tw,
                                           const typename XForm<V>::K& k) {
   FftStages2x<N, INV, 0, 1, AD, false, TWL, 1, V>::run(v, buf, t, tw, k);
 }

@@ -458,13 +458,13 @@ struct RowGeom {
 // VOX = true: the multislice hot path and plain row transforms only (optional row IFFT, optional
 // voxel transmission, row FFT, the optional field store and scale), so the point-source and
 // plasma code is not in the kernel.
-// DITH = true (with VOX, powers of two): the transforms use the slice's dithered tables
+// DITH = true (with VOX): the transforms use the slice's dithered tables
 // (twd1_inv / twd1_fwd, k_inv / k_fwd) in the single-sequence form of the split-pair arithmetic,
 // and the transmission is applied as the split-pair row kernel applies it, so the result is that
 // of row_x2_kernel with one row per thread group.
 template <int N, int ROWS, bool VOX = false, bool DITH = false>
 __global__ void __launch_bounds__(ROWS * FftPlan<N>::T, row_minb<N, ROWS>()) row_pass_kernel(const RowArgs a) {
-  static_assert(!DITH || (VOX && FftPlan<N>::POW2), "dithered rows: voxel hot path, power-of-two lengths");
+  static_assert(!DITH || VOX, "dithered rows: the voxel hot path");
   using P = FftPlan<N>;
   constexpr int T = P::T;
   constexpr int RF = P::entry_radix(false);   // forward entry == inverse exit mapping

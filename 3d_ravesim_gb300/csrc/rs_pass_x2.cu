@@ -97,8 +97,8 @@ cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const
   case N: return launch_rows_nvd<N, true, true>(a, s);
 
 // the dithered rows one per thread group also run at 16384, where a row pair does not fit shared
-// memory
-#define RS_D1_ONLY_ROW_SIZES(X) X(16384)
+// memory, and at the 3*2^k lengths (radix-24 first stage), which have no split-pair form
+#define RS_D1_ONLY_ROW_SIZES(X) X(16384) X(384) X(768) X(1536) X(3072) X(6144)
 
 cudaError_t launch_row_d1(int nx, const RowArgs& a, cudaStream_t s) {
   switch (nx) {
@@ -114,7 +114,7 @@ cudaError_t launch_row_d1(int nx, const RowArgs& a, cudaStream_t s) {
 cudaError_t launch_row_adjoint_d1(int nx, const RowArgs& a, cudaStream_t s) {
   switch (nx) {
     RS_X2_ROW_SIZES(RS_D1ADJ_CASE)
-    RS_D1_ONLY_ROW_SIZES(RS_D1ADJ_CASE)
+    RS_D1ADJ_CASE(16384)
     default: return cudaErrorInvalidValue;
   }
 }

@@ -293,8 +293,9 @@ int rs_plan_set_pipeline(rs_plan* plan, int mask);
 /*   RS_SCHED_SINGLE_ROWS (without RS_SCHED_COMP_ROWS) the dithered row passes hold one row per
  *                        thread group instead of two, in the single-sequence form of the same
  *                        arithmetic: the same results (up to the sign of zero) with half the
- *                        registers per thread. Rows of 16384 have only this form (a row pair
- *                        does not fit shared memory), so there the bit changes nothing. */
+ *                        registers per thread. Rows of 16384 (a row pair does not fit shared
+ *                        memory) and rows of 3*2^k in [384, 6144] (a radix-24 first stage) have
+ *                        only this form, so there the bit changes nothing. */
 #define RS_SCHED_SINGLE_ROWS 64
 /*   RS_SCHED_SINGLE_COLS (without RS_SCHED_COMP_COLS) the same for the dithered column passes:
  *                        one column per thread group (the strips of the pipelined single-sequence
