@@ -149,11 +149,13 @@ struct rs_plan {
   bool d1_only_rows = false;              // dithered rows exist only one per thread group (no split pairs)
   const volatile int* cancel = nullptr;   // host flag read between slices (rs_plan_set_cancel_flag)
   bool d1_cols = false;                   // dithered columns one per thread group (RS_SCHED_SINGLE_COLS)
+  bool d1_only_cols = false;              // dithered columns exist only one per thread group (3*2^k)
   void* twd_arena = nullptr;
   float4* twd_x = nullptr;
   float4* twd_y2 = nullptr;
   float2* twd1_x = nullptr;               // twd_x as (wr, wi) entries, for the single-sequence rows
-  float2* twd1_y2 = nullptr;              // twd_y2 likewise, for the single-sequence columns
+  float2* twd1_y2 = nullptr;              // twd_y2 likewise, for the single-sequence columns (for
+                                          // d1_only_cols: the stage-major table of ny)
   int twd_x_len = 0, twd_y2_len = 0;
   DftConsts kconst[kDitherTables];
   struct MapEntry {
@@ -368,8 +370,9 @@ cudaError_t run_col_ms(rs_plan* p, const ColArgs& ca, int j, bool* used, cudaStr
   const bool dense = depth == 1 || ca.bstride == static_cast<long long>(p->nx) * p->ny;
   // dithered columns: split pairs (col_x2_box strips) or one column per thread group
   // (col_pipe_box strips), the same values
-  const bool boxed = p->d1_cols ? col_pipe_box(p->ny, &w, &bh) : col_x2_box(p->ny, &w, &bh);
-  if (p->x2c_on && p->x2_cols && dense && ca.pitch == 0 && ca.tw4 == 0 && !ca.kyi && boxed &&
+  const bool single = p->d1_cols || p->d1_only_cols;
+  const bool boxed = single ? col_pipe_box(p->ny, &w, &bh) : col_x2_box(p->ny, &w, &bh);
+  if (p->x2c_on && (p->x2_cols || p->d1_only_cols) && dense && ca.pitch == 0 && ca.tw4 == 0 && !ca.kyi && boxed &&
       aligned16(ca.in) && aligned16(ca.out) && tensor_map_encoder()) {
     const CUtensorMap* mi = field_map(p, ca.in, w, bh, depth);
     if (mi) {
@@ -384,7 +387,7 @@ cudaError_t run_col_ms(rs_plan* p, const ColArgs& ca, int j, bool* used, cudaStr
         p->test_stall = 0;
         p->status_pending = true;
         *used = true;
-        return p->d1_cols ? launch_col_d1(p->ny, c, in_copy, *mo, p->status, s)
+        return single ? launch_col_d1(p->ny, c, in_copy, *mo, p->status, s)
                           : launch_col_x2(p->ny, c, in_copy, *mo, p->status, s);
       }
     }
@@ -960,14 +963,15 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
     return fail(RS_ECUDA, "twiddle setup: %s", cudaGetErrorString(e));
   }
   // dithered multislice passes: tables derived from the compensated ones (rows of 2^k and 3*2^k,
-  // split-pair columns of 2^k)
+  // split-pair columns of 2^k from the two-level table, single columns of 3*2^k from the stage table)
   if (fast) {
     int w = 0, bh = 0;
     p->x2_rows = row_x2_ok(nx);
     p->d1_only_rows = !p->x2_rows && row_d1_only(nx);
     p->x2_cols = col_x2_box(ny, &w, &bh) && p->tw2_y != nullptr;
+    p->d1_only_cols = !p->x2_cols && col_d1_only(ny);
     p->twd_x_len = p->x2_rows || p->d1_only_rows ? static_cast<int>(twx) : 0;
-    p->twd_y2_len = p->x2_cols ? static_cast<int>(tw2y) : 0;
+    p->twd_y2_len = p->x2_cols ? static_cast<int>(tw2y) : p->d1_only_cols ? static_cast<int>(twy) : 0;
     const size_t n = static_cast<size_t>(p->twd_x_len + p->twd_y2_len) * kDitherTables;
     if (n > 0) {
       // the split-pair (wr, wr, wi, wi) tables, then the same entries as (wr, wi)
@@ -978,7 +982,8 @@ int rs_plan_create(int nx, int ny, unsigned flags, rs_plan** out) {
         p->twd1_x = reinterpret_cast<float2*>(p->twd_x + n);
         p->twd1_y2 = p->twd1_x + static_cast<size_t>(p->twd_x_len) * kDitherTables;
         if (p->twd_x_len > 0) e = launch_dither_tables(p->tws_x, p->twd_x, p->twd_x_len, 0);
-        if (e == cudaSuccess && p->x2_cols) e = launch_dither_tables(p->tw2_y, p->twd_y2, p->twd_y2_len, 0);
+        if (e == cudaSuccess && p->twd_y2_len > 0)
+          e = launch_dither_tables(p->x2_cols ? p->tw2_y : p->tws_y, p->twd_y2, p->twd_y2_len, 0);
         if (e == cudaSuccess) e = launch_single_tables(p->twd_x, p->twd1_x, n, 0);
         if (e == cudaSuccess) e = cudaStreamSynchronize(0);
       }
@@ -1072,10 +1077,11 @@ int rs_plan_schedules(const rs_plan* p, int* masks, int cap, int* count) {
     // a direction without split-pair passes has only its single-sequence kernels; where the
     // split-pair passes run, the bits that choose among that direction's other kernels change nothing
     if ((m & RS_SCHED_COMP_ROWS) && !p->x2_rows && !p->d1_only_rows) continue;
-    if ((m & RS_SCHED_COMP_COLS) && !p->x2_cols) continue;
+    if ((m & RS_SCHED_COMP_COLS) && !p->x2_cols && !p->d1_only_cols) continue;
     if (!(m & RS_SCHED_COMP_ROWS) && (p->x2_rows || p->d1_only_rows) && (m & (RS_SCHED_PIPE_ROWS | RS_SCHED_ROW_GENERAL)))
       continue;
-    if (!(m & RS_SCHED_COMP_COLS) && p->x2_cols && (m & (RS_SCHED_PIPE_COLS | RS_SCHED_SPLIT_COLS))) continue;
+    if (!(m & RS_SCHED_COMP_COLS) && (p->x2_cols || p->d1_only_cols) && (m & (RS_SCHED_PIPE_COLS | RS_SCHED_SPLIT_COLS)))
+      continue;
     if ((m & RS_SCHED_SPLIT_COLS) && !p->split_ok) continue;
     if ((m & RS_SCHED_PIPE_ROWS) && !rows_pipe) continue;
     if ((m & RS_SCHED_PIPE_COLS) && !cols_pipe) continue;

@@ -85,11 +85,23 @@ cudaError_t launch_col_x2_n(const ColArgs& a, const CUtensorMap& in, const CUten
 #define RS_D1COL_CASE(N) \
   case N: return launch_col_pipe_n<N, true>(a, in, out, status, s);
 
+// the dithered columns one per thread group also run at the 3*2^k lengths of the column pipeline
+// (the one-level transform with a radix-24 first stage), which have no split-pair form
+#define RS_D1_ONLY_COL_SIZES(X) X(384) X(768) X(1536) X(3072) X(6144)
+
 cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
                           cudaStream_t s) {
   switch (ny) {
     RS_X2_COL_SIZES(RS_D1COL_CASE)
+    RS_D1_ONLY_COL_SIZES(RS_D1COL_CASE)
     default: return cudaErrorInvalidValue;
+  }
+}
+
+bool col_d1_only(int ny) {
+  switch (ny) {
+    RS_D1_ONLY_COL_SIZES(RS_X2OK_CASE)
+    default: return false;
   }
 }
 

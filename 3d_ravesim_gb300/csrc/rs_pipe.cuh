@@ -138,7 +138,7 @@ struct ColPipeGeom {
   // memory when they fit
   static constexpr int TW_LEN = L2 ? Fft2L<N>::TW_LEN : FftPlan<N>::TW_USED;
   static constexpr size_t TW_BYTES = static_cast<size_t>(TW_LEN) * (DITH ? sizeof(float2) : sizeof(float4));
-  static_assert(!DITH || L2, "dithered columns use the two-level transform");
+  static_assert(!DITH || L2 || !FftPlan<N>::POW2, "dithered 2^k columns use the two-level transform");
   // Three tile buffers when they fit beside the twiddle tables, else two: the twiddles in shared
   // memory matter more than the third buffer (the L1 left beside three 64 KB tiles cannot hold
   // the compensated tables of 4096-point columns). With DITH the third buffer is also given up
@@ -410,8 +410,11 @@ __global__ void __launch_bounds__(ColPipeGeom<N, DITH>::THREADS, 1)
     if (flags & COL_FWD) {
 #pragma unroll
       for (int e = 0; e < E; ++e) v[e] = col[slot_pos<N, RF>(t, e) * W];
-      if constexpr (DITH) {
+      if constexpr (DITH && G::L2) {
         fft2l_fwd2x<N, NatAddr, SwzAddr, TWL, W>(v, col, t, tw, k1);
+      } else if constexpr (DITH) {  // 3*2^k: the stage-major dithered table, radix-24 first stage
+        __syncthreads();
+        FftStages2x<N, false, 0, 1, SwzAddr, false, TWL, W, float2>::run(v, col, t, tw, k1);
       } else if constexpr (G::L2) {
         // the block exchange writes exactly the slots this thread just read: no barrier
         fft2l_fwd<N, NatAddr, SwzAddr, W, TWL>(v, col, t, tw);
@@ -456,7 +459,8 @@ __global__ void __launch_bounds__(ColPipeGeom<N, DITH>::THREADS, 1)
     }
     if (flags & COL_INV) {
       // two-level: the last exchange read exactly the slots this thread writes back
-      if constexpr (DITH) fft2l_inv2x<N, NatAddr, SwzAddr, TWL, W>(v, col, t, tw, k1);
+      if constexpr (DITH && G::L2) fft2l_inv2x<N, NatAddr, SwzAddr, TWL, W>(v, col, t, tw, k1);
+      else if constexpr (DITH) FftStages2x<N, true, 0, 1, SwzAddr, false, TWL, W, float2>::run(v, col, t, tw, k1);
       else if constexpr (G::L2) fft2l_inv<N, NatAddr, SwzAddr, W, TWL>(v, col, t, tw);
       else fft_seq<N, true, SwzAddr, W, TWL>(v, col, t, tw);
 #pragma unroll

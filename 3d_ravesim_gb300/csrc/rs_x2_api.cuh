@@ -14,12 +14,15 @@ cudaError_t launch_row_x2(int nx, const RowArgs& a, cudaStream_t s);
 cudaError_t launch_row_d1(int nx, const RowArgs& a, cudaStream_t s);
 // the adjoint row pass with the dithered tables (row_adjoint_kernel<N, ROWS, true>)
 cudaError_t launch_row_adjoint_d1(int nx, const RowArgs& a, cudaStream_t s);
-// sizes with dithered rows one per thread group but no split-pair rows (16384)
+// sizes with dithered rows one per thread group but no split-pair rows (16384, 3*2^k in [384, 6144])
 bool row_d1_only(int nx);
+// sizes with dithered columns one per thread group but no split-pair columns (3*2^k in [384, 6144])
+bool col_d1_only(int ny);
 cudaError_t launch_col_x2(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
                           cudaStream_t s);
 // the same column pass with one column per thread group (col_pipe_kernel<N, true>; strips and
-// boxes of col_pipe_box), for the split-pair column sizes; reads twd1 and kc
+// boxes of col_pipe_box), for the split-pair column sizes and the col_d1_only sizes; reads twd1
+// (the two-level table, or for col_d1_only the stage-major table) and kc
 cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
                           cudaStream_t s);
 // kDitherTables dithered copies of a compensated table of `len` entries (rs_fft2x.cuh)

@@ -55,12 +55,15 @@ def pass_kernels(mask: int, n: int) -> dict:
     """Kernel that runs the multislice row / column passes of an n x n plan under a schedule mask."""
     x2_rows = n in (256, 512, 1024, 2048, 4096, 8192)
     x2_cols = n in (256, 512, 1024, 2048, 4096)
-    if x2_rows and not mask & 16:
-        rows = "row_pass_kernel" if mask & 64 else "row_x2_kernel"  # 64: dithered, one row per group
+    single = (384, 768, 1536, 3072, 6144)  # dithered rows / columns only one per thread group
+    if (x2_rows or n in single + (16384,)) and not mask & 16:
+        # 64: dithered, one row per group (the only dithered form at 16384 and 3*2^k)
+        rows = "row_pass_kernel" if mask & 64 or not x2_rows else "row_x2_kernel"
     else:
         rows = "row_pipe_kernel" if mask & 1 else "row_pass_kernel"
-    if x2_cols and not mask & 32:
-        cols = "col_pipe_kernel" if mask & 128 else "col_x2_pipe_kernel"  # 128: dithered, one column per group
+    if (x2_cols or n in single) and not mask & 32:
+        # 128: dithered, one column per group (the only dithered form at 3*2^k)
+        cols = "col_pipe_kernel" if mask & 128 or not x2_cols else "col_x2_pipe_kernel"
     else:
         cols = "col_pipe_kernel" if mask & 2 and not mask & 8 else "col_pass_kernel"
     return {"row_pass": rows, "col_pass": cols}
@@ -212,20 +215,21 @@ def l2_flush_buffer(torch, device):
     return torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)
 
 
-def schedule_name(mask: int) -> str:
-    """Readable form of a pass-schedule mask (bits: 1 pipelined rows, 2 pipelined columns,
-    4 general row kernel, 8 split columns, 16 / 32 single-sequence compensated rows / columns
-    instead of the split-pair passes, for the sizes that have them, 64 / 128 the dithered rows /
-    columns one per thread group)."""
+def schedule_name(mask: int, n: int = 4096) -> str:
+    """Readable form of a pass-schedule mask of an n x n plan (bits: 1 pipelined rows, 2 pipelined
+    columns, 4 general row kernel, 8 split columns, 16 / 32 single-sequence compensated rows /
+    columns instead of the dithered passes, for the sizes that have them, 64 / 128 the dithered
+    rows / columns one per thread group, the only dithered form at 16384 (rows) and 3*2^k)."""
+    single = n in (384, 768, 1536, 3072, 6144)
     if mask & 16:
         rows = "rows:pipelined" if mask & 1 else ("rows:per-block" if mask & 4 else "rows:per-block-voxel")
     else:
-        rows = "rows:dithered-single" if mask & 64 else "rows:split-pair"
+        rows = "rows:dithered-single" if mask & 64 or single or n == 16384 else "rows:split-pair"
     if mask & 32:
         cols = "cols:pipelined" if mask & 2 else "cols:per-block"
         if mask & 8:
             cols = "cols:split-3-pass (last slice " + cols.split(":")[1] + ")"
-    elif mask & 128:
+    elif mask & 128 or single:
         cols = "cols:dithered-single"
     else:
         cols = "cols:split-pair"
@@ -737,8 +741,8 @@ def run_ours(args):
                        "l2": "256 MiB buffer written between timed steps (flush outside the events)",
                        "parallelism": f"replicas x{world} (one field per GPU)"},
             "roofline": roofline, "gpu_launches": launches, "clocks": clocks.summary(),
-            "schedule": {"mask": tuned.mask, "passes": schedule_name(tuned.mask),
-                         "tuned_ms_per_schedule": {schedule_name(m): round(t, 3)
+            "schedule": {"mask": tuned.mask, "passes": schedule_name(tuned.mask, n),
+                         "tuned_ms_per_schedule": {schedule_name(m, n): round(t, 3)
                                                    for m, t in sorted(tuned.timings_ms.items())},
                          "tuned_on": f"{tuned.slices} seeded voxel slices at {n}^2" if tuned.slices else "given",
                          "max_rel_diff_between_schedules": max(tuned.rel_diff.values(), default=None)}}

@@ -29,6 +29,8 @@ def test_schedule_lists(rs, cuda):
                                                           64, 96, 98, 128, 144, 145, 148, 192]  # no split
     assert lib.plan_for(8192, 64, cuda).schedules() == [0, 16, 17, 20, 64]  # split-pair rows, 64-point columns
     assert lib.plan_for(16384, 64, cuda).schedules() == [0, 16, 20]  # dithered rows only one per thread group
+    # 3*2^k: dithered rows and columns only one per thread group (radix-24 first stage)
+    assert lib.plan_for(3072, 3072, cuda).schedules() == [0, 16, 17, 20, 32, 34, 48, 49, 50, 51, 52, 54]
     assert lib.plan_for(72, 40, cuda).schedules() == [0]  # direct-DFT sizes have one schedule
     p = lib.plan_for(1024, 1024, cuda)
     old = p.schedule()
