@@ -353,7 +353,7 @@ cudaError_t run_col(rs_plan* p, const ColArgs& ca, cudaStream_t s) {
         p->status_pending = true;
         c.test_stall = p->test_stall;
         p->test_stall = 0;
-        return launch_col_pipe(p->ny, c, in_copy, *mo, p->status, s);
+        return launch_col_pipe(p->ny, c, in_copy, *mo, StripBox{w, bh}, p->status, s);
       }
     }
   }
@@ -369,9 +369,9 @@ cudaError_t run_col_ms(rs_plan* p, const ColArgs& ca, int j, bool* used, cudaStr
   const int depth = ca.batches > 1 ? ca.batches : 1;
   const bool dense = depth == 1 || ca.bstride == static_cast<long long>(p->nx) * p->ny;
   // dithered columns: split pairs (col_x2_box strips) or one column per thread group
-  // (col_pipe_box strips), the same values
+  // (col_d1_box strips), the same values
   const bool single = p->d1_cols || p->d1_only_cols;
-  const bool boxed = single ? col_pipe_box(p->ny, &w, &bh) : col_x2_box(p->ny, &w, &bh);
+  const bool boxed = single ? col_d1_box(p->ny, &w, &bh) : col_x2_box(p->ny, &w, &bh);
   if (p->x2c_on && (p->x2_cols || p->d1_only_cols) && dense && ca.pitch == 0 && ca.tw4 == 0 && !ca.kyi && boxed &&
       aligned16(ca.in) && aligned16(ca.out) && tensor_map_encoder()) {
     const CUtensorMap* mi = field_map(p, ca.in, w, bh, depth);
@@ -387,8 +387,8 @@ cudaError_t run_col_ms(rs_plan* p, const ColArgs& ca, int j, bool* used, cudaStr
         p->test_stall = 0;
         p->status_pending = true;
         *used = true;
-        return single ? launch_col_d1(p->ny, c, in_copy, *mo, p->status, s)
-                          : launch_col_x2(p->ny, c, in_copy, *mo, p->status, s);
+        return single ? launch_col_d1(p->ny, c, in_copy, *mo, StripBox{w, bh}, p->status, s)
+                      : launch_col_x2(p->ny, c, in_copy, *mo, StripBox{w, bh}, p->status, s);
       }
     }
   }

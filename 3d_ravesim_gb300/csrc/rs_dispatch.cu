@@ -54,10 +54,10 @@ cudaError_t launch_row_pipe(int nx, const RowArgs& a, int* status, cudaStream_t 
   return is_pow2(nx) ? launch_row_pipe_pow2(nx, a, status, s) : launch_row_pipe_pow3(nx, a, status, s);
 }
 
-cudaError_t launch_col_pipe(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
-                            cudaStream_t s) {
-  return is_pow2(ny) ? launch_col_pipe_pow2(ny, a, in, out, status, s)
-                     : launch_col_pipe_pow3(ny, a, in, out, status, s);
+cudaError_t launch_col_pipe(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, StripBox box,
+                            int* status, cudaStream_t s) {
+  return is_pow2(ny) ? launch_col_pipe_pow2(ny, a, in, out, box, status, s)
+                     : launch_col_pipe_pow3(ny, a, in, out, box, status, s);
 }
 
 }  // namespace rs

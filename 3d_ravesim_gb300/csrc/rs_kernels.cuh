@@ -95,6 +95,13 @@ struct RowArgs {
   const float2* twd1_fwd;
 };
 
+// Box of the tensor maps a pipelined column pass reads and writes: columns per box (the strip
+// width) and rows per copy. A launcher runs only when it equals its kernel's strip geometry, so
+// a copy can never deliver more bytes than the strip buffer it lands in.
+struct StripBox {
+  int w = 0, bh = 0;
+};
+
 struct ColArgs {
   const float2* in;
   float2* out;

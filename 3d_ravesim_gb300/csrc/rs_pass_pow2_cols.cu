@@ -54,13 +54,13 @@ int stage_twiddle_len_pow2(int n) {
 }
 
 #define RS_COLPIPE_CASE(N) \
-  case N: return launch_col_pipe_n<N>(a, in, out, status, s);
+  case N: return launch_col_pipe_n<N>(a, in, out, box, status, s);
 
 #define RS_COLBOX_CASE(N) \
   case N: *w = ColPipeGeom<N>::W; *bh = ColPipeGeom<N>::BH; return true;
 
 cudaError_t launch_col_pipe_pow2(int n, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out,
-                                 int* status, cudaStream_t s) {
+                                 StripBox box, int* status, cudaStream_t s) {
   switch (n) {
     RS_POW2_PIPE_COL(RS_COLPIPE_CASE)
     default: return cudaErrorInvalidValue;

@@ -44,9 +44,10 @@ constexpr int col_x2_minb() {
 }
 
 template <int N, int MINB = col_x2_minb<N>()>
-cudaError_t launch_col_x2_n(const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
-                            cudaStream_t s) {
+cudaError_t launch_col_x2_n(const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, StripBox box,
+                            int* status, cudaStream_t s) {
   using G = ColX2Geom<N, MINB>;
+  if (box.w != G::W || box.bh != G::BH) return cudaErrorInvalidValue;
   static unsigned configured = 0;
   static int grid_cache[32];
   int dev = 0;
@@ -76,25 +77,35 @@ cudaError_t launch_col_x2_n(const ColArgs& a, const CUtensorMap& in, const CUten
 #define RS_X2ROW_CASE(N) \
   case N: return launch_row_x2_n<N>(a, s);
 #define RS_X2COL_CASE(N) \
-  case N: return launch_col_x2_n<N>(a, in, out, status, s);
+  case N: return launch_col_x2_n<N>(a, in, out, box, status, s);
 #define RS_X2BOX_CASE(N) \
   case N: *w = ColX2Geom<N>::W; *bh = ColX2Geom<N>::BH; return true;
 #define RS_X2OK_CASE(N) \
   case N: return true;
 
 #define RS_D1COL_CASE(N) \
-  case N: return launch_col_pipe_n<N, true>(a, in, out, status, s);
+  case N: return launch_col_pipe_n<N, true>(a, in, out, box, status, s);
+#define RS_D1BOX_CASE(N) \
+  case N: *w = ColPipeGeom<N, true>::W; *bh = ColPipeGeom<N, true>::BH; return true;
 
 // the dithered columns one per thread group also run at the 3*2^k lengths of the column pipeline
 // (the one-level transform with a radix-24 first stage), which have no split-pair form
 #define RS_D1_ONLY_COL_SIZES(X) X(384) X(768) X(1536) X(3072) X(6144)
 
-cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
-                          cudaStream_t s) {
+cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, StripBox box,
+                          int* status, cudaStream_t s) {
   switch (ny) {
     RS_X2_COL_SIZES(RS_D1COL_CASE)
     RS_D1_ONLY_COL_SIZES(RS_D1COL_CASE)
     default: return cudaErrorInvalidValue;
+  }
+}
+
+bool col_d1_box(int ny, int* w, int* bh) {
+  switch (ny) {
+    RS_X2_COL_SIZES(RS_D1BOX_CASE)
+    RS_D1_ONLY_COL_SIZES(RS_D1BOX_CASE)
+    default: return false;
   }
 }
 
@@ -152,8 +163,8 @@ bool row_x2_ok(int nx) {
   }
 }
 
-cudaError_t launch_col_x2(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
-                          cudaStream_t s) {
+cudaError_t launch_col_x2(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, StripBox box,
+                          int* status, cudaStream_t s) {
   switch (ny) {
     RS_X2_COL_SIZES(RS_X2COL_CASE)
     default: return cudaErrorInvalidValue;

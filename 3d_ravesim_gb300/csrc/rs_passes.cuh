@@ -216,9 +216,10 @@ cudaError_t launch_row_pipe_n(const RowArgs& a, int* status, cudaStream_t s) {
 }
 
 template <int N, bool DITH = false>
-cudaError_t launch_col_pipe_n(const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
-                              cudaStream_t s) {
+cudaError_t launch_col_pipe_n(const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, StripBox box,
+                              int* status, cudaStream_t s) {
   using G = ColPipeGeom<N, DITH>;
+  if (box.w != G::W || box.bh != G::BH) return cudaErrorInvalidValue;
   static unsigned configured = 0;
   static int grid_cache[32];
   int dev = 0;
@@ -252,10 +253,11 @@ cudaError_t launch_col_pipe_n(const ColArgs& a, const CUtensorMap& in, const CUt
 cudaError_t launch_row_pipe_pow2(int n, const RowArgs& a, int* status, cudaStream_t s);
 cudaError_t launch_row_pipe_pow3(int n, const RowArgs& a, int* status, cudaStream_t s);
 cudaError_t launch_col_pipe_pow2(int n, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out,
-                                 int* status, cudaStream_t s);
+                                 StripBox box, int* status, cudaStream_t s);
 cudaError_t launch_col_pipe_pow3(int n, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out,
-                                 int* status, cudaStream_t s);
-// box of the column pipeline for length n: columns per strip and rows per copy; false if none.
+                                 StripBox box, int* status, cudaStream_t s);
+// box of the compensated column pipeline for length n: columns per strip and rows per copy;
+// false if none.
 bool col_pipe_box_pow2(int n, int* w, int* bh);
 bool col_pipe_box_pow3(int n, int* w, int* bh);
 bool row_pipe_ok_pow2(int n);

@@ -126,7 +126,29 @@ struct ColPipeGeom {
 #endif
   // threads per strip: 256 at 1536 and 2048 (column passes 12 % and 10 % faster, measured),
   // RS_COLPIPE_THREADS (512) elsewhere (256 was 7 % slower at 1024 and 3072)
-  static constexpr int THR = (N == 1536 || N == 2048) ? 256 : RS_COLPIPE_THREADS;
+  // The dithered 3*2^k columns (the one-level transform with a radix-24 first stage) choose their
+  // blocks per SM (MINB), threads per strip and strip buffers (NB) per size below; every other
+  // form runs one block per SM with two or three strip buffers.
+  // At 1536 and 3072 two 256-thread blocks per SM with one strip buffer each (the other block
+  // computes while one waits for its next strip): column passes 26.6 / 92.0 us against 28.8 /
+  // 95.0 with one block and two or three buffers; three blocks per SM (80 registers) spill and
+  // took 29.2 / 95.2 us. RS_COLPIPE_D3_MINB / RS_COLPIPE_D3_THREADS force one choice for every
+  // 3*2^k size.
+  static constexpr bool D3 = DITH && !FftPlan<N>::POW2;
+  static constexpr bool D3_PAIR = D3 && (N == 1536 || N == 3072);
+#ifdef RS_COLPIPE_D3_MINB
+  static constexpr int MINB = D3 ? RS_COLPIPE_D3_MINB : 1;
+#else
+  static constexpr int MINB = D3_PAIR ? 2 : 1;
+#endif
+#ifndef RS_COLPIPE_D3_THREADS
+#define RS_COLPIPE_D3_THREADS 0
+#endif
+  static constexpr int THR = (D3 && RS_COLPIPE_D3_THREADS > 0) ? RS_COLPIPE_D3_THREADS
+                             : (D3_PAIR || N == 1536 || N == 2048) ? 256
+                                                                   : RS_COLPIPE_THREADS;
+  // shared memory of one block when MINB blocks share an SM (228 KB, 1 KB reserved per block)
+  static constexpr size_t BUDGET = MINB == 1 ? 227 * 1024 : 228 * 1024 / MINB - 1024;
   // columns per strip (>= 2: 16-byte boxes) for about THR threads
   static constexpr int W = T >= THR / 2 ? 2 : THR / T;
   static constexpr int BH = box_rows(N);                      // rows per tensor-copy box
@@ -143,18 +165,26 @@ struct ColPipeGeom {
   // memory matter more than the third buffer (the L1 left beside three 64 KB tiles cannot hold
   // the compensated tables of 4096-point columns). With DITH the third buffer is also given up
   // for ey in shared memory.
+#ifndef RS_COLPIPE_D3_NB
+#define RS_COLPIPE_D3_NB 0
+#endif
 #ifdef RS_COLPIPE_NB
   static constexpr int NB = RS_COLPIPE_NB;
 #else
-  static constexpr int NB =
-      (3 * TILE * 8 + TW_BYTES + (DITH ? N * sizeof(float2) : 0) + 64 <= 227 * 1024) ? 3 : 2;
+  static constexpr int NB = (D3 && RS_COLPIPE_D3_NB > 0) ? RS_COLPIPE_D3_NB
+                            : MINB >= 2                  ? 1
+                            : (3 * TILE * 8 + TW_BYTES + (DITH ? N * sizeof(float2) : 0) + 64 <= BUDGET) ? 3
+                                                                                                        : 2;
 #endif
   static constexpr size_t TILES_BYTES = static_cast<size_t>(NB) * TILE * sizeof(float2);
 #ifndef RS_COLPIPE_TW_SMEM
 #define RS_COLPIPE_TW_SMEM 1
 #endif
-  static constexpr bool TW_SMEM =
-      RS_COLPIPE_TW_SMEM && TW_LEN > 0 && TILES_BYTES + TW_BYTES + 64 <= 227 * 1024;
+#ifndef RS_COLPIPE_D3_TW_SMEM
+#define RS_COLPIPE_D3_TW_SMEM 1
+#endif
+  static constexpr bool TW_SMEM = RS_COLPIPE_TW_SMEM && (!D3 || RS_COLPIPE_D3_TW_SMEM) && TW_LEN > 0 &&
+                                  TILES_BYTES + TW_BYTES + 64 <= BUDGET;
   // ey in shared memory too when it fits, stored in the register order of the forward exit
   // mapping (entry e * T + t), so that a warp's reads are consecutive
 #ifndef RS_COLPIPE_EY_SMEM
@@ -162,7 +192,7 @@ struct ColPipeGeom {
 #endif
   static constexpr size_t EY_BYTES = static_cast<size_t>(N) * sizeof(float2);
   static constexpr bool EY_SMEM =
-      RS_COLPIPE_EY_SMEM && TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + EY_BYTES + 64 <= 227 * 1024;
+      RS_COLPIPE_EY_SMEM && TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + EY_BYTES + 64 <= BUDGET;
   static constexpr size_t SMEM =
       TILES_BYTES + (TW_SMEM ? TW_BYTES : 0) + (EY_SMEM ? EY_BYTES : 0) + NB * sizeof(uint64_t);
 };
@@ -316,7 +346,7 @@ __global__ void __launch_bounds__(RowPipeGeom<N>::THREADS, RowPipeGeom<N>::MINB)
 // split-pair arithmetic, H and the mask applied as col_x2_pipe_kernel applies them: the result is
 // that kernel's, with one column per thread group.
 template <int N, bool DITH = false>
-__global__ void __launch_bounds__(ColPipeGeom<N, DITH>::THREADS, 1)
+__global__ void __launch_bounds__(ColPipeGeom<N, DITH>::THREADS, ColPipeGeom<N, DITH>::MINB)
     col_pipe_kernel(const ColArgs a, const __grid_constant__ CUtensorMap map_in,
                     const __grid_constant__ CUtensorMap map_out, int* status) {
   using P = FftPlan<N>;
@@ -391,13 +421,15 @@ __global__ void __launch_bounds__(ColPipeGeom<N, DITH>::THREADS, 1)
     // iteration; the copy is started halfway through this strip's work (below), by when that
     // store has long been read out, so no thread waits for it.
     auto prefetch_next = [&]() {
-      if (threadIdx.x == 0 && next < ntiles) {
-        bulk_wait_read<G::NB - 2>();
-        const int bn = (i + 1) % G::NB;
-        mbar_arrive_expect(&bars[bn], TILE_BYTES);
-        for (int k = 0; k < N / G::BH; ++k)
-          tma_load_3d(tiles + bn * G::TILE + k * G::BH * W, &map_in, (next % strips) * W, k * G::BH,
-                      next / strips, &bars[bn]);
+      if constexpr (G::NB >= 2) {
+        if (threadIdx.x == 0 && next < ntiles) {
+          bulk_wait_read<G::NB - 2>();
+          const int bn = (i + 1) % G::NB;
+          mbar_arrive_expect(&bars[bn], TILE_BYTES);
+          for (int k = 0; k < N / G::BH; ++k)
+            tma_load_3d(tiles + bn * G::TILE + k * G::BH * W, &map_in, (next % strips) * W, k * G::BH,
+                        next / strips, &bars[bn]);
+        }
       }
     };
     ok = __syncthreads_and(mbar_wait_bounded(&bars[b], (i / G::NB) & 1, status));
@@ -476,6 +508,16 @@ __global__ void __launch_bounds__(ColPipeGeom<N, DITH>::THREADS, 1)
       for (int k = 0; k < N / G::BH; ++k)
         tma_store_3d(&map_out, (tile % strips) * W, k * G::BH, fb, tb + k * G::BH * W);
       bulk_commit();
+      if constexpr (G::NB == 1) {
+        // one buffer: the next strip lands in it once this store has read it out (the other
+        // blocks of the SM compute meanwhile)
+        if (next < ntiles) {
+          bulk_wait_read<0>();
+          mbar_arrive_expect(&bars[0], TILE_BYTES);
+          for (int k = 0; k < N / G::BH; ++k)
+            tma_load_3d(tiles + k * G::BH * W, &map_in, (next % strips) * W, k * G::BH, next / strips, &bars[0]);
+        }
+      }
     }
   }
   if (threadIdx.x == 0) bulk_wait_all();

@@ -18,13 +18,17 @@ cudaError_t launch_row_adjoint_d1(int nx, const RowArgs& a, cudaStream_t s);
 bool row_d1_only(int nx);
 // sizes with dithered columns one per thread group but no split-pair columns (3*2^k in [384, 6144])
 bool col_d1_only(int ny);
-cudaError_t launch_col_x2(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
-                          cudaStream_t s);
+// box: the one the maps were encoded with (col_x2_box); any other is refused
+cudaError_t launch_col_x2(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, StripBox box,
+                          int* status, cudaStream_t s);
 // the same column pass with one column per thread group (col_pipe_kernel<N, true>; strips and
-// boxes of col_pipe_box), for the split-pair column sizes and the col_d1_only sizes; reads twd1
+// boxes of col_d1_box), for the split-pair column sizes and the col_d1_only sizes; reads twd1
 // (the two-level table, or for col_d1_only the stage-major table) and kc
-cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, int* status,
-                          cudaStream_t s);
+cudaError_t launch_col_d1(int ny, const ColArgs& a, const CUtensorMap& in, const CUtensorMap& out, StripBox box,
+                          int* status, cudaStream_t s);
+// box of the dithered one-column pass (its own strip geometry, which may differ from the
+// compensated pipeline's); false if none
+bool col_d1_box(int ny, int* w, int* bh);
 // kDitherTables dithered copies of a compensated table of `len` entries (rs_fft2x.cuh)
 cudaError_t launch_dither_tables(const float4* comp, float4* out, int len, cudaStream_t s);
 // (wr, wi) of each of `n` split-pair entries (wr, wr, wi, wi)

@@ -70,7 +70,7 @@ def test_multislice_pipeline_bit_identical(rs, cuda, n, pitch):
 
 
 @pytest.mark.parametrize("nx,ny", [(4096, 4096), (1024, 1536), (2048, 2048), (512, 512), (8192, 1024), (16384, 256),
-                                   (1536, 1024), (3072, 512)])
+                                   (1536, 1024), (3072, 512), (512, 3072)])
 def test_split_pair_passes_match_compensated_passes(rs, cuda, nx, ny):
     """The split-pair multislice passes (two rows / two columns per thread group in packed f32x2
     arithmetic, dithered twiddle tables) against the single-sequence passes with compensated
