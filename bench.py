@@ -555,6 +555,29 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
     n_full = len(full.items)
     del per_item, stacked, plain_full
     torch.cuda.empty_cache()
+    # per grid size: 64 items of one size (4 x 4 jittered sources x 4 energies of the same spectrum,
+    # so the stacks hold 16 items as in the full batch), stacked against the plain loop, to show
+    # where the ratio comes from
+    by_size = {}
+    for n in b.info["sizes"]:
+        one = ms.shell_batch(n_sources_side=4, n_energies=4, sizes=(n,))
+        t = {}
+        for name, streams, kw in (("stacked", 2, {"stacked": True}), ("plain", 1, {"plain": True})):
+            r = ms.BatchRunner(one, device, streams=streams)
+            r.run(one.items[:2], **({"plain": True} if name == "plain" else {}))
+            if name == "stacked":
+                r.run(one.items[:16], stacked=True)
+            r.zero()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r.run(**kw)
+            torch.cuda.synchronize()
+            t[name] = time.perf_counter() - t0
+            del r
+        torch.cuda.empty_cache()
+        by_size[str(n)] = {"stacked_items_per_s": round(64 / t["stacked"], 2),
+                           "plain_loop_items_per_s": round(64 / t["plain"], 2),
+                           "speedup": round(t["plain"] / t["stacked"], 2)}
     slices = b.sample.grid.shape[0]
     res = {"case": f"{items} of 1024 items, sizes {b.info['sizes']}, {slices} slices each",
            "fused_items_per_s": round(items / out["fused_s"], 2),
@@ -570,7 +593,8 @@ def multisim_cost(rs, torch, device, items: int = 128) -> dict:
                           "plain_loop_items_per_s": round(n_full / full_out["plain_loop_s"], 2),
                           "speedup": round(full_out["plain_loop_s"] /
                                            min(full_out["fused_s"], full_out["fused_stacked_s"]), 2),
-                          **full_out}}
+                          **full_out},
+           "by_size_64_items": by_size}
     return res
 
 

@@ -70,13 +70,15 @@ def test_multislice_pipeline_bit_identical(rs, cuda, n, pitch):
 
 
 @pytest.mark.parametrize("nx,ny", [(4096, 4096), (1024, 1536), (2048, 2048), (512, 512), (8192, 1024), (16384, 256),
-                                   (1536, 1024), (3072, 512), (512, 3072)])
+                                   (1536, 1024), (3072, 512), (512, 3072), (768, 384), (384, 6144), (6144, 768)])
 def test_split_pair_passes_match_compensated_passes(rs, cuda, nx, ny):
     """The split-pair multislice passes (two rows / two columns per thread group in packed f32x2
     arithmetic, dithered twiddle tables) against the single-sequence passes with compensated
     twiddles on the same 12-slice voxel run: equal to FP32 rounding (both are within the FP64
     accuracy bound; their roundings differ). The dithered rows (bit 64) and columns (bit 128) one
-    per thread group give the split-pair passes' values exactly."""
+    per thread group give the split-pair passes' values exactly. Rows of 16384 and rows and
+    columns of 3*2^k have only the one-per-group dithered form (radix-24 first stage): there the
+    default schedule runs it and is held to the same bound against the compensated passes."""
     wl = rs.convert_energy_wavelength(25000.0)
     dx = 0.25e-6
     pitch = 0.7e-6
