@@ -299,7 +299,8 @@ int rs_plan_set_pipeline(rs_plan* plan, int mask);
 #define RS_SCHED_SINGLE_ROWS 64
 /*   RS_SCHED_SINGLE_COLS (without RS_SCHED_COMP_COLS) the same for the dithered column passes:
  *                        one column per thread group (the strips of the pipelined single-sequence
- *                        column pass), the split-pair columns' results. */
+ *                        column pass), the split-pair columns' results. Columns of 3*2^k in
+ *                        [384, 6144] have only this form, so there the bit changes nothing. */
 #define RS_SCHED_SINGLE_COLS 128
 int rs_plan_set_schedule(rs_plan* plan, int mask);
 int rs_plan_get_schedule(const rs_plan* plan, int* mask);
