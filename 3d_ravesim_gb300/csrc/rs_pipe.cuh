@@ -180,10 +180,15 @@ struct ColPipeGeom {
 #ifndef RS_COLPIPE_TW_SMEM
 #define RS_COLPIPE_TW_SMEM 1
 #endif
-#ifndef RS_COLPIPE_D3_TW_SMEM
-#define RS_COLPIPE_D3_TW_SMEM 1
+  // At 1536 and 3072 (two blocks per SM) ey takes the shared memory beside the strip and the
+  // table is read through L1: column passes 24.7 / 83.3 us against 26.9 / 91.5 with the table in
+  // shared memory and ey through L1. RS_COLPIPE_D3_TW_SMEM forces one choice for every 3*2^k size.
+#ifdef RS_COLPIPE_D3_TW_SMEM
+  static constexpr bool D3_TW_SMEM = RS_COLPIPE_D3_TW_SMEM;
+#else
+  static constexpr bool D3_TW_SMEM = !D3_PAIR;
 #endif
-  static constexpr bool TW_SMEM = RS_COLPIPE_TW_SMEM && (!D3 || RS_COLPIPE_D3_TW_SMEM) && TW_LEN > 0 &&
+  static constexpr bool TW_SMEM = RS_COLPIPE_TW_SMEM && (!D3 || D3_TW_SMEM) && TW_LEN > 0 &&
                                   TILES_BYTES + TW_BYTES + 64 <= BUDGET;
   // ey in shared memory too when it fits, stored in the register order of the forward exit
   // mapping (entry e * T + t), so that a warp's reads are consecutive
