@@ -221,18 +221,18 @@ def schedule_name(mask: int, n: int = 4096) -> str:
     columns instead of the dithered passes, for the sizes that have them, 64 / 128 the dithered
     rows / columns one per thread group, the only dithered form at 16384 (rows) and 3*2^k)."""
     single = n in (384, 768, 1536, 3072, 6144)
-    if mask & 16:
-        rows = "rows:pipelined" if mask & 1 else ("rows:per-block" if mask & 4 else "rows:per-block-voxel")
+    x2_rows = n in (256, 512, 1024, 2048, 4096, 8192)
+    x2_cols = n in (256, 512, 1024, 2048, 4096)
+    if (x2_rows or single or n == 16384) and not mask & 16:
+        rows = "rows:dithered-single" if mask & 64 or not x2_rows else "rows:split-pair"
     else:
-        rows = "rows:dithered-single" if mask & 64 or single or n == 16384 else "rows:split-pair"
-    if mask & 32:
+        rows = "rows:pipelined" if mask & 1 else ("rows:per-block" if mask & 4 else "rows:per-block-voxel")
+    if (x2_cols or single) and not mask & 32:
+        cols = "cols:dithered-single" if mask & 128 or not x2_cols else "cols:split-pair"
+    else:
         cols = "cols:pipelined" if mask & 2 else "cols:per-block"
         if mask & 8:
             cols = "cols:split-3-pass (last slice " + cols.split(":")[1] + ")"
-    elif mask & 128 or single:
-        cols = "cols:dithered-single"
-    else:
-        cols = "cols:split-pair"
     return f"{rows},{cols}"
 
 

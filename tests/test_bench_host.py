@@ -32,3 +32,24 @@ def test_reference_arm_json_line():
 def test_reference_arm_other_ranks_do_nothing():
     r = run({"RANK": "1", "WORLD_SIZE": "2", "LOCAL_RANK": "1"})
     assert r.returncode == 0 and r.stdout.strip() == ""
+
+
+def test_pass_kernel_names_follow_the_schedule_rules():
+    """The kernels the bench line names for each pass: split pairs where they exist, the dithered
+    one-per-group kernels where they are the only dithered form (rows of 16384 and 3*2^k, columns
+    of 3*2^k), the compensated kernels under bits 16 / 32."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    assert bench.pass_kernels(64, 4096) == {"row_pass": "row_pass_kernel", "col_pass": "col_x2_pipe_kernel"}
+    assert bench.pass_kernels(0, 4096) == {"row_pass": "row_x2_kernel", "col_pass": "col_x2_pipe_kernel"}
+    assert bench.pass_kernels(192, 4096) == {"row_pass": "row_pass_kernel", "col_pass": "col_pipe_kernel"}
+    assert bench.pass_kernels(0, 3072) == {"row_pass": "row_pass_kernel", "col_pass": "col_pipe_kernel"}
+    assert bench.pass_kernels(48, 3072) == {"row_pass": "row_pass_kernel", "col_pass": "col_pass_kernel"}
+    assert bench.pass_kernels(51, 3072) == {"row_pass": "row_pipe_kernel", "col_pass": "col_pipe_kernel"}
+    assert bench.pass_kernels(0, 16384)["row_pass"] == "row_pass_kernel"
+    assert bench.schedule_name(0, 3072) == "rows:dithered-single,cols:dithered-single"
+    assert bench.schedule_name(64, 4096) == "rows:dithered-single,cols:split-pair"
+    assert bench.schedule_name(48, 3072) == "rows:per-block-voxel,cols:per-block"
+    assert bench.schedule_name(16, 16384) == "rows:per-block-voxel,cols:per-block"
+    assert bench.schedule_name(8, 16384) == "rows:dithered-single,cols:split-3-pass (last slice per-block)"
+    assert bench.schedule_name(42, 4096) == "rows:split-pair,cols:split-3-pass (last slice pipelined)"
