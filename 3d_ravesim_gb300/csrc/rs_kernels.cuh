@@ -143,6 +143,12 @@ struct ColArgs {
 // result) with x = pi h formed from a two-float pi; otherwise sincospif.
 constexpr float kPiHi = 3.14159274101257324219f;
 constexpr float kPiLo = -8.74227766e-08f;
+// The library sine/cosine and expm1 of the rarely taken branches below, kept out of line so that
+// the fully unrolled transmission loops of the row passes carry one call instead of one inlined
+// copy per pixel (the same functions, so the same bits).
+static __device__ __noinline__ void sincospif_ool(float h, float* s, float* c) { sincospif(h, s, c); }
+static __device__ __noinline__ float expm1f_ool(float x) { return expm1f(x); }
+
 __device__ __forceinline__ void sincospi_small(float h, float* s, float* c) {
   if (fabsf(h) < 0.0625f) {
     const float x = fmaf(h, kPiHi, h * kPiLo);
@@ -151,7 +157,7 @@ __device__ __forceinline__ void sincospi_small(float h, float* s, float* c) {
                            -1.6666667e-01f), 1.0f);
     *c = fmaf(x2, fmaf(x2, fmaf(x2, fmaf(x2, 2.4801587e-05f, -1.3888889e-03f), 4.1666667e-02f), -0.5f), 1.0f);
   } else {
-    sincospif(h, s, c);
+    sincospif_ool(h, s, c);
   }
 }
 
@@ -171,7 +177,7 @@ __device__ __forceinline__ float2 material_factor(float delta, float beta, float
   // the library expm1f otherwise
   const float em1 = fabsf(x) < 0.015625f
                         ? x * fmaf(x, fmaf(x, fmaf(x, 0.041666666666666667f, 0.16666666666666667f), 0.5f), 1.0f)
-                        : expm1f(x);
+                        : expm1f_ool(x);
   const float amp = 1.0f + em1;
   return make_float2(amp * c, -amp * s);
 }
@@ -210,8 +216,8 @@ __device__ __forceinline__ cp2 material_factor2(float2 dA, float2 dB, float a) {
   const float2 q = p_fma(x, make_float2(0.041666666666666667f, 0.041666666666666667f),
                          make_float2(0.16666666666666667f, 0.16666666666666667f));
   float2 em1 = p_mul(x, p_fma(x, p_fma(x, q, make_float2(0.5f, 0.5f)), make_float2(1.f, 1.f)));
-  if (!(fabsf(x.x) < 0.015625f)) em1.x = expm1f(x.x);
-  if (!(fabsf(x.y) < 0.015625f)) em1.y = expm1f(x.y);
+  if (!(fabsf(x.x) < 0.015625f)) em1.x = expm1f_ool(x.x);
+  if (!(fabsf(x.y) < 0.015625f)) em1.y = expm1f_ool(x.y);
   const float2 amp = p_add(make_float2(1.f, 1.f), em1);
   return {p_mul(amp, c), p_mul(amp, ns)};
 }
