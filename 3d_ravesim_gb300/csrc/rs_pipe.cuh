@@ -124,16 +124,14 @@ struct ColPipeGeom {
 #ifndef RS_COLPIPE_THREADS
 #define RS_COLPIPE_THREADS 512
 #endif
-  // threads per strip: 256 at 1536 and 2048 (column passes 12 % and 10 % faster, measured),
-  // RS_COLPIPE_THREADS (512) elsewhere (256 was 7 % slower at 1024 and 3072)
-  // The dithered 3*2^k columns (the one-level transform with a radix-24 first stage) choose their
-  // blocks per SM (MINB), threads per strip and strip buffers (NB) per size below; every other
-  // form runs one block per SM with two or three strip buffers.
-  // At 1536 and 3072 two 256-thread blocks per SM with one strip buffer each (the other block
-  // computes while one waits for its next strip): column passes 26.6 / 92.0 us against 28.8 /
-  // 95.0 with one block and two or three buffers; three blocks per SM (80 registers) spill and
-  // took 29.2 / 95.2 us. RS_COLPIPE_D3_MINB / RS_COLPIPE_D3_THREADS force one choice for every
-  // 3*2^k size.
+  // Threads per strip: 256 at 1536 and 2048 (compensated column passes 12 % and 10 % faster,
+  // measured), RS_COLPIPE_THREADS (512) elsewhere (256 was 7 % slower at 1024 and 3072 there).
+  // Every form runs one block per SM with two or three strip buffers, except the dithered 3*2^k
+  // columns (the one-level transform with a radix-24 first stage) at 1536 and 3072: two
+  // 256-thread blocks per SM with one strip buffer each (the other block computes while one
+  // waits for its next strip), column passes 26.6 / 92.0 us against 28.8 / 95.0 with one block
+  // and two or three buffers; three blocks per SM (80 registers) spill and took 29.2 / 95.2 us.
+  // RS_COLPIPE_D3_MINB / RS_COLPIPE_D3_THREADS force one choice for every 3*2^k size.
   static constexpr bool D3 = DITH && !FftPlan<N>::POW2;
   static constexpr bool D3_PAIR = D3 && (N == 1536 || N == 3072);
 #ifdef RS_COLPIPE_D3_MINB
